@@ -1,0 +1,179 @@
+/*
+ * rascil_gb300 -- C-ABI of the GB300 (sm_103a) w-stacking gridder/degridder.
+ *
+ * This is the drop-in replacement for the two ducc0 calls that RASCIL's
+ * ng imaging path makes:
+ *
+ *   ducc0.wgridder.ms2dirty  rascil/processing_components/imaging/ng.py:232-248, 259-275
+ *   ducc0.wgridder.dirty2ms  rascil/processing_components/imaging/ng.py:91-103, 108-120
+ *
+ * with the same operator (ducc0 0.24.0 semantics: flipped u/w as ng.py
+ * passes them, image axis order [x][y], pixel centre at n/2, 1/n factor
+ * when w-stacking).  Work is split into a plan (uvw-dependent: w range,
+ * bucket sort of visibilities into uv tiles) and calls that reuse it, so
+ * that several polarisations, invert + predict, and repeated autograd
+ * calls share one sort.
+ *
+ * Conventions
+ *  - every pointer named *_dev is a device pointer; host pointers say so;
+ *  - every call is asynchronous on the caller's CUDA stream (cudaStream_t
+ *    passed as void*), except gb_plan_create, which synchronises the
+ *    stream once to read the w range back;
+ *  - the library never frees caller memory; scratch memory comes from a
+ *    caller-provided workspace (gb_plan_workspace_size / gb_plan_bind);
+ *  - every entry point returns a gb_status; gb_last_error_string() gives a
+ *    message for the calling thread's last failure.  No C++ exception
+ *    crosses this boundary.
+ */
+#ifndef RASCIL_GB300_H
+#define RASCIL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  ng.py asserts (ng.py:46,71,158) and wg.py raises
+ * ValueError (wg.py:52-54,79-85); here invalid arguments come back as
+ * GB_ERR_INVALID_ARG and the Python layer raises ValueError. */
+typedef enum {
+  GB_OK = 0,
+  GB_ERR_INVALID_ARG = 1,
+  GB_ERR_NOT_BOUND = 2,
+  GB_ERR_WORKSPACE = 3,
+  GB_ERR_CUDA = 4,
+  GB_ERR_CUFFT = 5,
+  GB_ERR_TIMEOUT = 6,
+  GB_ERR_INTERNAL = 7
+} gb_status;
+
+typedef enum { GB_FP32 = 0, GB_FP64 = 1 } gb_precision;
+
+/* Image memory layout.  GB_LAYOUT_XY is ducc0's dirty[x][y] (what
+ * ms2dirty returns and dirty2ms takes).  GB_LAYOUT_YX is RASCIL's
+ * pixels[..., y, x] (ng.py passes model.T to ducc0, ng.py:94,249), so the
+ * Python layer needs no transposes. */
+typedef enum { GB_LAYOUT_XY = 0, GB_LAYOUT_YX = 1 } gb_layout;
+
+/* Element type of the optional flags array (nonzero = flagged).  RASCIL's
+ * BlockVisibility flags are int64 (memory_data_models.py:1502-1523). */
+typedef enum { GB_FLAGS_NONE = 0, GB_FLAGS_U8 = 1, GB_FLAGS_I64 = 2 } gb_flags_type;
+
+typedef struct {
+  int64_t nrows;       /* R: uvw rows (times x baselines)                      */
+  int32_t nchan;       /* C: frequency channels gridded by this plan           */
+  int32_t npol;        /* P: image polarisations gridded together (1, 2, 4)    */
+  int32_t npix_x;      /* image size along x (ducc0 npix_x), even, >= 16      */
+  int32_t npix_y;      /* image size along y (ducc0 npix_y), even, >= 16      */
+  double pixsize_x;    /* radians                                              */
+  double pixsize_y;    /* radians                                              */
+  double epsilon;      /* requested accuracy (ducc0 epsilon)                   */
+  int32_t do_wstacking;/* ducc0 do_wstacking                                   */
+  int32_t precision;   /* gb_precision                                         */
+  double sigma;        /* grid oversampling; 0 = default (2.0)                 */
+  int32_t support;     /* kernel support W; 0 = smallest W meeting epsilon     */
+  int32_t tile;        /* uv tile side in cells; 0 = default                   */
+  int32_t slab;        /* w-planes per bucket slab; 0 = default                */
+  int64_t grid_budget_bytes; /* memory for one batch of w-planes; 0 = default  */
+} gb_plan_params;
+
+/* Geometry the planner chose; all host values. */
+typedef struct {
+  int32_t support, ngrid_x, ngrid_y, nplanes, planes_per_batch, tile, slab;
+  double beta, sigma, dw, w_lo, w_hi, tc;
+  int64_t nitems, nbuckets, workspace_bytes;
+} gb_plan_info;
+
+typedef struct gb_plan gb_plan;
+
+/* Host-only planning: the geometry for a given w range, without a GPU.
+ * Mirrors what gb_plan_create computes after its w-range reduction. */
+int gb_plan_geometry(const gb_plan_params *params, double w_lo, double w_hi,
+                     gb_plan_info *info_out);
+
+/* Create a plan for the visibility coordinates uvw_dev [nrows][3] (metres,
+ * float64) at freq_dev [nchan] (Hz, float64).  Reduces the w range on
+ * the device and synchronises `stream` once.  Replaces the per-call setup
+ * inside ducc0.wgridder.ms2dirty/dirty2ms (ng.py:91-120,232-275). */
+int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
+                   const double *freq_dev, void *stream, gb_plan **plan_out);
+
+/* Bytes of device scratch the plan needs (16-byte aligned start). */
+int gb_plan_workspace_size(const gb_plan *plan, size_t *bytes_out);
+
+/* Bind scratch memory and run the device-side bucket sort of all
+ * (row, channel) items into (w-slab, uv-tile) buckets.  Asynchronous. */
+int gb_plan_bind(gb_plan *plan, void *workspace_dev, size_t workspace_bytes,
+                 void *stream);
+
+int gb_plan_info_get(const gb_plan *plan, gb_plan_info *info_out);
+
+/* Verification export of the bucket sort: for every item i = row * nchan +
+ * chan, its bucket id (slab-major, then v-tile, then u-tile), first support
+ * cell (p0, q0, k0) and offsets (du, dv, dwf) as stored.  Any output may
+ * be NULL.  No counterpart in the reference (ducc0 keeps its index
+ * internal); it lets tests prove the device sort is bit-exact. */
+int gb_plan_export_items(const gb_plan *plan, uint32_t *bucket_dev, int32_t *cell_dev,
+                         double *frac_dev, void *stream);
+
+/* Release host resources (cuFFT plans).  Never frees the workspace. */
+int gb_plan_destroy(gb_plan *plan);
+
+/* Invert: dirty image from visibilities.  Replaces ducc0 ms2dirty
+ * (ng.py:232-248 MFS, 259-275 per channel) for all npol polarisations
+ * in one pass.
+ *   vis_dev     [nrows][nchan][npol_vis] complex64 (GB_FP32) or complex128
+ *   wgt_dev     [nrows][nchan][npol_vis] float32 / float64, or NULL (= 1)
+ *   flags_dev   [nrows][nchan][npol_vis] of flags_type, or NULL
+ *   polmat_host npol x npol_vis complex (re, im interleaved, float64):
+ *               vis-frame -> image-frame matrix, or NULL for identity
+ *               (convert_pol_frame, rascil/data_models/polarisation.py:367-419)
+ *   psf         nonzero: grid (1, 0, ...) instead of the data (ng.py:223-225)
+ *   dirty_dev   [npol] images of float32 / float64 in `layout`
+ *   sumwt_dev   [npol] float64 sums of (flagged) weights, or NULL
+ */
+int gb_plan_ms2dirty(gb_plan *plan, const void *vis_dev, int32_t npol_vis,
+                     const void *wgt_dev, const void *flags_dev,
+                     int32_t flags_type, const double *polmat_host, int32_t psf,
+                     void *dirty_dev, int32_t layout, double *sumwt_dev,
+                     void *stream);
+
+/* Predict: visibilities from a model image.  Replaces ducc0 dirty2ms
+ * (ng.py:91-103 MFS, 108-120 per channel) for all npol polarisations.
+ *   dirty_dev   [npol] real images (float32 / float64) in `layout`
+ *   wgt_dev     [nrows][nchan][npol_vis] or NULL (ng.py passes None)
+ *   polmat_host npol_vis x npol complex: image-frame -> vis-frame, or NULL
+ *   vis_dev     [nrows][nchan][npol_vis] complex64 / complex128 (written)
+ */
+int gb_plan_dirty2ms(gb_plan *plan, const void *dirty_dev, int32_t layout,
+                     const void *wgt_dev, const double *polmat_host,
+                     int32_t npol_vis, void *vis_dev, void *stream);
+
+/* One-shot ducc0-shaped calls (single polarisation, [nrows][nchan] data,
+ * dirty in [npix_x][npix_y]); allocate scratch with cudaMallocAsync on
+ * `stream` and free it before returning.  Same arguments and meaning as
+ * ducc0.wgridder.ms2dirty / dirty2ms as called at ng.py:232-248 / 91-103. */
+int gb_ms2dirty(const double *uvw_dev, const double *freq_dev, int64_t nrows,
+                int32_t nchan, const void *ms_dev, const void *wgt_dev,
+                int32_t npix_x, int32_t npix_y, double pixsize_x,
+                double pixsize_y, double epsilon, int32_t do_wstacking,
+                int32_t precision, void *dirty_dev, void *stream);
+
+int gb_dirty2ms(const double *uvw_dev, const double *freq_dev, int64_t nrows,
+                int32_t nchan, const void *dirty_dev, const void *wgt_dev,
+                int32_t npix_x, int32_t npix_y, double pixsize_x,
+                double pixsize_y, double epsilon, int32_t do_wstacking,
+                int32_t precision, void *ms_dev, void *stream);
+
+/* Message for the calling thread's last non-GB_OK status. */
+const char *gb_last_error_string(void);
+
+/* Library version string. */
+const char *gb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RASCIL_GB300_H */

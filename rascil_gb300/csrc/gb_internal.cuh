@@ -1,0 +1,220 @@
+// Internal definitions shared by the gridder's translation units.
+//
+// Algorithm (restated from the published method behind ducc0.wgridder,
+// which rascil/processing_components/imaging/ng.py:91-120,232-275 calls):
+// exponential-of-semicircle (ES) kernel gridding on a sigma-oversampled
+// uv grid, w-stacking with the same kernel along w, 2-D FFTs per w-plane,
+// a w-screen per plane and a final correction by the kernel's Fourier
+// transform.  The data layout is GB300-first:
+//
+//  * visibilities are addressed as items (row, channel); the plan sorts
+//    them once into buckets (w-slab, uv-tile) and stores one compact
+//    record per item in bucket order (ItemF / ItemD);
+//  * uv-grids are [plane][pol][v][u] complex, u fastest, so a pixel row of
+//    the image is a contiguous run of the FFT output;
+//  * grids carry a (-1)^(p+q) checkerboard, which moves the image to the
+//    central block of the FFT output (no fftshift pass);
+//  * images are [pol][y][x] internally (RASCIL's order), x fastest.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/rascil_gb300.h"
+
+namespace gb {
+
+constexpr double kSpeedOfLight = 299792458.0;  // rascil/phyconst.py:6
+constexpr int kThreads = 256;                   // block size of the tile kernels
+constexpr int kWarps = kThreads / 32;
+constexpr int kChunkItems = 256;                // items per work chunk
+constexpr int kMaxSupport = 16;
+constexpr int kMaxQuad = 48;                    // Gauss-Legendre nodes (half interval)
+
+struct Geom {
+  int nx, ny;        // image
+  int ngx, ngy;      // oversampled grid
+  double dx, dy;     // pixel size (rad)
+  int W;             // kernel support (cells)
+  double beta;       // ES shape
+  double sigma;
+  int do_w;
+  double tc;         // centre of the image's (n-1) range
+  double dw;         // w-plane spacing (wavelengths)
+  double w_lo, w_hi; // visibility w range (wavelengths)
+  int nplanes;
+  int T;             // uv tile side (cells)
+  int S;             // w-planes per bucket slab
+  int ntu, ntv, nslabs;
+  int64_t nbuckets;
+  int64_t R;         // rows
+  int C;             // channels
+  int NP;            // image polarisations
+  uint32_t nitems;   // R * C
+  int B;             // planes per batch
+  int nquad;         // quadrature nodes for the w correction
+};
+
+// Item record in bucket order.  `loc` packs the item's first support cell
+// inside its tile (bits 0-7 u, 8-15 v) and its first w-plane inside its
+// slab (bits 16-23).  du, dv, dwf are the offsets of the item's continuous
+// grid coordinate from its first support cell (in (W/2-1, W/2]); ph is
+// exp(-2 pi i w tc), the rotation that centres the (n-1) band.
+struct __align__(16) ItemF {
+  uint32_t idx, loc;
+  float du, dv, dwf, pad;
+  float2 ph;
+};
+struct __align__(16) ItemD {
+  uint32_t idx, loc;
+  double du, dv, dwf;
+  double2 ph;
+};
+
+template <typename R> struct Traits;
+template <> struct Traits<float> {
+  using C = float2;
+  using Item = ItemF;
+};
+template <> struct Traits<double> {
+  using C = double2;
+  using Item = ItemD;
+};
+
+// A unit of work for the tile kernels: up to kChunkItems consecutive items
+// of one bucket.
+struct Chunk {
+  uint32_t begin, end, bucket, pad;
+};
+
+// Polarisation conversion matrix (nout x nin complex, row-major); the
+// identity is flagged so kernels skip the multiply.
+struct PolMat {
+  int nout, nin, identity, pad;
+  double re[16], im[16];
+};
+
+// ---------------------------------------------------------------------
+// Per-item coordinates, FP64, with every rounding step explicit so the
+// result is bit-identical to the CPU restatement (no FMA contraction).
+struct Coord {
+  int p0, q0;      // first support cell, wrapped into [0, ng)
+  int k0;          // first w-plane
+  double du, dv, dwf;
+  double w;        // w in wavelengths
+};
+
+__host__ __device__ inline double gb_mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+__host__ __device__ inline double gb_add(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+__host__ __device__ inline double gb_sub(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+__host__ __device__ inline double gb_div(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __ddiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+
+__host__ __device__ inline void item_coord(const Geom &g, const double *uvw,
+                                           const double *freq, uint32_t i,
+                                           Coord &o) {
+  const uint32_t r = i / (uint32_t)g.C;
+  const uint32_t c = i - r * (uint32_t)g.C;
+  const double s = gb_div(freq[c], kSpeedOfLight);
+  const double u = gb_mul(uvw[3 * (size_t)r + 0], s);
+  const double v = gb_mul(uvw[3 * (size_t)r + 1], s);
+  const double w = gb_mul(uvw[3 * (size_t)r + 2], s);
+  const double halfW = 0.5 * g.W;
+  double fu = gb_mul(u, g.dx);
+  fu = gb_sub(fu, floor(fu));
+  const double U = gb_mul(fu, (double)g.ngx);
+  const double p0 = ceil(gb_sub(U, halfW));
+  o.du = gb_sub(U, p0);
+  double fv = gb_mul(v, g.dy);
+  fv = gb_sub(fv, floor(fv));
+  const double V = gb_mul(fv, (double)g.ngy);
+  const double q0 = ceil(gb_sub(V, halfW));
+  o.dv = gb_sub(V, q0);
+  int ip = (int)p0, iq = (int)q0;
+  ip = ip < 0 ? ip + g.ngx : (ip >= g.ngx ? ip - g.ngx : ip);
+  iq = iq < 0 ? iq + g.ngy : (iq >= g.ngy ? iq - g.ngy : iq);
+  o.p0 = ip;
+  o.q0 = iq;
+  o.w = w;
+  if (g.do_w) {
+    const double a = gb_div(gb_sub(w, g.w_lo), g.dw);
+    const double k0 = ceil(a);
+    o.dwf = gb_add(gb_sub(a, k0), halfW);
+    int ik = (int)k0;
+    const int kmax = g.nplanes - g.W;
+    ik = ik < 0 ? 0 : (ik > kmax ? kmax : ik);
+    o.k0 = ik;
+  } else {
+    o.dwf = 0.0;
+    o.k0 = 0;
+  }
+}
+
+__host__ __device__ inline uint32_t bucket_of(const Geom &g, const Coord &o) {
+  const uint32_t tu = (uint32_t)(o.p0 / g.T);
+  const uint32_t tv = (uint32_t)(o.q0 / g.T);
+  const uint32_t sl = (uint32_t)(o.k0 / g.S);
+  return (sl * (uint32_t)g.ntv + tv) * (uint32_t)g.ntu + tu;
+}
+
+// ---------------------------------------------------------------------
+// ES kernel at support-normalised x in [-1, 1).
+__device__ __forceinline__ float es_kernel(float x, float beta) {
+  const float t = 1.0f - x * x;
+  return t > 0.0f ? expf(beta * (sqrtf(t) - 1.0f)) : 0.0f;
+}
+__device__ __forceinline__ double es_kernel(double x, double beta) {
+  const double t = 1.0 - x * x;
+  return t > 0.0 ? exp(beta * (sqrt(t) - 1.0)) : 0.0;
+}
+
+__device__ __forceinline__ void sincos_2pi(float frac, float *s, float *c) {
+  sincospif(2.0f * frac, s, c);
+}
+__device__ __forceinline__ void sincos_2pi(double frac, double *s, double *c) {
+  sincospi(2.0 * frac, s, c);
+}
+
+// n - 1 for pixel (ix, iy), cancellation-free form.
+__device__ __forceinline__ double pixel_nm1(const Geom &g, int ix, int iy) {
+  const double x = (double)(ix - g.nx / 2) * g.dx;
+  const double y = (double)(iy - g.ny / 2) * g.dy;
+  const double r2 = x * x + y * y;
+  return -r2 / (1.0 + sqrt(1.0 - r2));
+}
+
+// Phase (in turns, reduced to [-1/2, 1/2]) of w-plane k at offset tprime.
+__device__ __forceinline__ double plane_turns(const Geom &g, int k, double tprime) {
+  const double wk = g.w_lo + ((double)k - 0.5 * g.W) * g.dw;
+  const double ph = wk * tprime;
+  return ph - rint(ph);
+}
+
+// Error reporting -------------------------------------------------------
+void set_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+}  // namespace gb

@@ -1,0 +1,452 @@
+// Invert (ms2dirty): visibilities -> dirty image.
+//
+// Per call:   k_prep_vis    gather every item's visibilities in bucket order,
+//                           apply flags, weights, the pol-frame matrix and the
+//                           w-centring rotation; sum the weights per pol.
+// Per batch of w-planes:
+//             k_grid        one CTA per work chunk (<= 256 items of one
+//                           (slab, tile) bucket): the tile's sub-grid lives in
+//                           shared memory, each warp spreads one item at a
+//                           time over its W x W support (kernel values per
+//                           support row/column, exchanged by warp shuffles),
+//                           then the sub-grid is flushed to the HBM grid with
+//                           vector atomics.  Sparse chunks skip the sub-grid.
+//             cuFFT         2-D c2c, e^{+2 pi i}, batched over planes x pols
+//             k_screen_acc  reads the central block of each plane, applies the
+//                           w-screen exp(-2 pi i w_k (n-1-tc)) and accumulates.
+// Once:       k_finalize    multiply by the correction image, write the
+//                           requested layout.
+#include <cufft.h>
+
+#include "gb_plan.cuh"
+
+namespace gb {
+
+template <typename R, int NP>
+__global__ void __launch_bounds__(kThreads)
+    k_prep_vis(const Geom g, const typename Traits<R>::Item *__restrict__ items,
+               const typename Traits<R>::C *__restrict__ vis, int npv,
+               const R *__restrict__ wgt, const void *__restrict__ flags, int ftype,
+               const PolMat pm, int psf, typename Traits<R>::C *__restrict__ cvis,
+               double *__restrict__ sumwt) {
+  using C = typename Traits<R>::C;
+  double wsum[NP];
+#pragma unroll
+  for (int p = 0; p < NP; ++p) wsum[p] = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.nitems; j += stride) {
+    const auto it = items[j];
+    const size_t base = (size_t)it.idx * npv;
+    R m[4];
+    for (int q = 0; q < 4; ++q) m[q] = (R)1;
+    if (ftype == GB_FLAGS_U8) {
+      const uint8_t *f = reinterpret_cast<const uint8_t *>(flags) + base;
+      for (int q = 0; q < npv; ++q) m[q] = f[q] ? (R)0 : (R)1;
+    } else if (ftype == GB_FLAGS_I64) {
+      const int64_t *f = reinterpret_cast<const int64_t *>(flags) + base;
+      for (int q = 0; q < npv; ++q) m[q] = f[q] ? (R)0 : (R)1;
+    }
+    C out[NP];
+    if (psf) {
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {
+        out[p].x = p == 0 ? (R)1 : (R)0;
+        out[p].y = (R)0;
+      }
+    } else {
+      C v[4];
+      for (int q = 0; q < 4; ++q) {
+        v[q].x = (R)0;
+        v[q].y = (R)0;
+      }
+      for (int q = 0; q < npv; ++q) {
+        const C x = vis[base + q];
+        v[q].x = x.x * m[q];
+        v[q].y = x.y * m[q];
+      }
+      if (pm.identity) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) out[p] = v[p];
+      } else {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          R re = 0, im = 0;
+          for (int q = 0; q < npv; ++q) {
+            const R mr = (R)pm.re[p * pm.nin + q], mi = (R)pm.im[p * pm.nin + q];
+            re += mr * v[q].x - mi * v[q].y;
+            im += mr * v[q].y + mi * v[q].x;
+          }
+          out[p].x = re;
+          out[p].y = im;
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const R w = (wgt ? wgt[base + p] : (R)1) * m[p];
+      wsum[p] += (double)w;
+      const R re = out[p].x * w, im = out[p].y * w;
+      C o;
+      o.x = re * it.ph.x - im * it.ph.y;
+      o.y = re * it.ph.y + im * it.ph.x;
+      cvis[(size_t)j * NP + p] = o;
+    }
+  }
+  if (sumwt) {
+    __shared__ double red[kWarps][NP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      double x = wsum[p];
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0) red[warp][p] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NP) {
+      double x = 0.0;
+      for (int w = 0; w < kWarps; ++w) x += red[w][threadIdx.x];
+      atomicAdd(&sumwt[threadIdx.x], x);
+    }
+  }
+}
+
+__device__ __forceinline__ void grid_add(float2 *dst, float re, float im) {
+  atomicAdd(dst, make_float2(re, im));
+}
+__device__ __forceinline__ void grid_add(double2 *dst, double re, double im) {
+  atomicAdd(&dst->x, re);
+  atomicAdd(&dst->y, im);
+}
+
+// Slab range [s_lo, s_hi] whose items reach planes [b0, b0 + nb).
+__device__ __forceinline__ void batch_slabs(const Geom &g, int b0, int nb, int &s_lo,
+                                            int &s_hi) {
+  const int lo = b0 - (g.S + g.W - 2);
+  s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
+  s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
+}
+
+template <typename R, int NP>
+__global__ void __launch_bounds__(kThreads)
+    k_grid(const Geom g, const typename Traits<R>::Item *__restrict__ items,
+           const typename Traits<R>::C *__restrict__ cvis, const Chunk *__restrict__ chunks,
+           const uint32_t *__restrict__ chunk_off, int b0, int nb,
+           typename Traits<R>::C *__restrict__ grid, uint32_t *__restrict__ counter) {
+  using C = typename Traits<R>::C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R *sg = reinterpret_cast<R *>(smem_raw);  // [NP][SW*SW] x (re, im)
+  const int W = g.W, T = g.T, SW = T + W - 1, SW2 = SW * SW;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const R scale = (R)2 / (R)W;
+  const R beta = (R)g.beta;
+  const int ntiles = g.ntu * g.ntv;
+  const size_t plane = (size_t)g.ngx * g.ngy;
+  int s_lo, s_hi;
+  batch_slabs(g, b0, nb, s_lo, s_hi);
+  const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
+  const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
+  __shared__ uint32_t s_ci;
+  for (;;) {
+    if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t ci = s_ci;
+    __syncthreads();
+    if (ci >= c_end) break;
+    const Chunk ch = chunks[ci];
+    const int slab = (int)(ch.bucket / (uint32_t)ntiles);
+    const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
+    const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
+    const int kbase = slab * g.S;
+    const int k_lo = max(kbase, b0);
+    const int k_hi = min(min(kbase + g.S + W - 1, g.nplanes), b0 + nb);
+    const int n = (int)(ch.end - ch.begin);
+    const bool direct = n * W * W < SW2;
+    for (int k = k_lo; k < k_hi; ++k) {
+      C *gplane = grid + (size_t)(k - b0) * NP * plane;
+      if (!direct) {
+        for (int i = threadIdx.x; i < NP * SW2 * 2; i += kThreads) sg[i] = (R)0;
+        __syncthreads();
+      }
+      for (uint32_t j = ch.begin + warp; j < ch.end; j += kWarps) {
+        const auto it = items[j];
+        const int aw = k - (kbase + (int)((it.loc >> 16) & 0xffu));
+        if (aw < 0 || aw >= W) continue;
+        const R fw = g.do_w ? es_kernel(((R)aw - it.dwf) * scale, beta) : (R)1;
+        C c[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          c[p] = cvis[(size_t)j * NP + p];
+          c[p].x *= fw;
+          c[p].y *= fw;
+        }
+        R kl = (R)0;
+        if (lane < W)
+          kl = es_kernel(((R)lane - it.du) * scale, beta);
+        else if (lane >= 16 && lane < 16 + W)
+          kl = es_kernel(((R)(lane - 16) - it.dv) * scale, beta);
+        const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
+        const int ncell = W * W;
+        for (int base = 0; base < ncell; base += 32) {
+          const int cell = base + lane;
+          const int b = cell / W, a = cell - b * W;
+          const R ku = __shfl_sync(0xffffffffu, kl, a);
+          const R kv = __shfl_sync(0xffffffffu, kl, 16 + min(b, W - 1));
+          if (cell < ncell) {
+            const R kk = ku * kv;
+            if (direct) {
+              int p = tu * T + lu + a;
+              if (p >= g.ngx) p -= g.ngx;
+              int q = tv * T + lv + b;
+              if (q >= g.ngy) q -= g.ngy;
+              const R sgn = ((p + q) & 1) ? (R)-1 : (R)1;
+              const R f = sgn * kk;
+#pragma unroll
+              for (int pol = 0; pol < NP; ++pol)
+                grid_add(&gplane[pol * plane + (size_t)q * g.ngx + p], f * c[pol].x,
+                         f * c[pol].y);
+            } else {
+              const int si = (lv + b) * SW + (lu + a);
+#pragma unroll
+              for (int pol = 0; pol < NP; ++pol) {
+                atomicAdd(&sg[2 * (pol * SW2 + si)], kk * c[pol].x);
+                atomicAdd(&sg[2 * (pol * SW2 + si) + 1], kk * c[pol].y);
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+      if (!direct) {
+        for (int i = threadIdx.x; i < SW2; i += kThreads) {
+          const int y = i / SW, x = i - y * SW;
+          int p = tu * T + x;
+          while (p >= g.ngx) p -= g.ngx;
+          int q = tv * T + y;
+          while (q >= g.ngy) q -= g.ngy;
+          const R sgn = ((p + q) & 1) ? (R)-1 : (R)1;
+#pragma unroll
+          for (int pol = 0; pol < NP; ++pol) {
+            const R re = sg[2 * (pol * SW2 + i)], im = sg[2 * (pol * SW2 + i) + 1];
+            if (re != (R)0 || im != (R)0)
+              grid_add(&gplane[pol * plane + (size_t)q * g.ngx + p], sgn * re, sgn * im);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+template <typename R, int NP>
+__global__ void __launch_bounds__(kThreads)
+    k_screen_acc(const Geom g, const typename Traits<R>::C *__restrict__ grid, int b0, int nb,
+                 R *__restrict__ acc, int first) {
+  using C = typename Traits<R>::C;
+  const int64_t npix = (int64_t)g.nx * g.ny;
+  const int ox = (g.ngx - g.nx) / 2, oy = (g.ngy - g.ny) / 2;
+  const size_t plane = (size_t)g.ngx * g.ngy;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += stride) {
+    const int iy = (int)(i / g.nx), ix = (int)(i - (int64_t)iy * g.nx);
+    R a[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) a[p] = first ? (R)0 : acc[p * npix + i];
+    const size_t gi = (size_t)(iy + oy) * g.ngx + (ix + ox);
+    if (g.do_w) {
+      const double tp = pixel_nm1(g, ix, iy) - g.tc;
+      for (int j = 0; j < nb; ++j) {
+        const double turns = plane_turns(g, b0 + j, tp);
+        R s, c;
+        sincos_2pi((R)turns, &s, &c);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const C v = grid[((size_t)j * NP + p) * plane + gi];
+          a[p] += v.x * c + v.y * s;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int p = 0; p < NP; ++p) a[p] += grid[(size_t)p * plane + gi].x;
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[p * npix + i] = a[p];
+  }
+}
+
+// out = acc * corr in the requested layout (32 x 32 tiles, transposed
+// through shared memory for ducc0's [x][y] order).
+template <typename R>
+__global__ void k_finalize(const Geom g, const R *__restrict__ acc, const R *__restrict__ corr,
+                           R *__restrict__ out, int layout) {
+  __shared__ R tile[32][33];
+  const int64_t npix = (int64_t)g.nx * g.ny;
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32, p = blockIdx.z;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int iy = by + j, ix = bx + threadIdx.x;
+    if (iy < g.ny && ix < g.nx) {
+      const int64_t i = (int64_t)iy * g.nx + ix;
+      const R v = acc[p * npix + i] * corr[i];
+      if (layout == GB_LAYOUT_YX)
+        out[p * npix + i] = v;
+      else
+        tile[j][threadIdx.x] = v;
+    }
+  }
+  if (layout == GB_LAYOUT_XY) {
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+      const int ix = bx + j, iy = by + threadIdx.x;
+      if (iy < g.ny && ix < g.nx) out[p * npix + (int64_t)ix * g.ny + iy] = tile[threadIdx.x][j];
+    }
+  }
+}
+
+template <typename R> static cufftResult fft_exec(cufftHandle h, void *data, int dir);
+template <> cufftResult fft_exec<float>(cufftHandle h, void *data, int dir) {
+  return cufftExecC2C(h, (cufftComplex *)data, (cufftComplex *)data, dir);
+}
+template <> cufftResult fft_exec<double>(cufftHandle h, void *data, int dir) {
+  return cufftExecZ2Z(h, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, dir);
+}
+
+int run_fft(gb_plan *p, int nb, void *data, int dir, cudaStream_t s) {
+  cufftHandle h = nb == p->g.B ? p->fft_full : p->fft_rem;
+  if (cufftSetStream(h, s) != CUFFT_SUCCESS) {
+    set_error("cufftSetStream failed");
+    return GB_ERR_CUFFT;
+  }
+  const cufftResult r = p->precision == GB_FP64 ? fft_exec<double>(h, data, dir)
+                                                : fft_exec<float>(h, data, dir);
+  if (r != CUFFT_SUCCESS) {
+    const cudaError_t e = cudaGetLastError();
+    size_t sz = 0;
+    cufftGetSize(h, &sz);
+    // retry through a fresh, self-allocating plan to tell plan from data problems
+    cufftHandle h2;
+    long long n[2] = {p->g.ngy, p->g.ngx};
+    size_t ws2 = 0;
+    cufftCreate(&h2);
+    cufftResult r2 = cufftMakePlanMany64(h2, 2, n, nullptr, 1, 0, nullptr, 1, 0,
+                                         p->precision == GB_FP64 ? CUFFT_Z2Z : CUFFT_C2C,
+                                         (long long)nb * p->g.NP, &ws2);
+    cufftResult r3 = CUFFT_SUCCESS;
+    if (r2 == CUFFT_SUCCESS) {
+      cufftSetStream(h2, s);
+      r3 = p->precision == GB_FP64 ? fft_exec<double>(h2, data, dir)
+                                   : fft_exec<float>(h2, data, dir);
+    }
+    cufftDestroy(h2);
+    set_error("cufftExec failed (cufft status %d, CUDA %s, handle %d, nb %d, B %d, work %zu "
+              "reserved %zu, data %p, ws %p, fresh plan make %d exec %d)",
+              (int)r, cudaGetErrorString(e), (int)h, nb, p->g.B, sz, p->fft_work_bytes, data,
+              (void *)(p->ws + p->off_fftwork), (int)r2, (int)r3);
+    return GB_ERR_CUFFT;
+  }
+  GB_LAUNCH_CHECK("cufftExec");
+  return GB_OK;
+}
+
+size_t tile_smem_bytes(const gb_plan *p) {
+  const int SW = p->g.T + p->g.W - 1;
+  return (size_t)p->g.NP * SW * SW * 2 * real_bytes(p->precision);
+}
+
+template <typename R, int NP>
+static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
+                         const void *flags, int ftype, const PolMat &pm, int psf, void *dirty,
+                         int layout, double *sumwt, cudaStream_t s) {
+  using C = typename Traits<R>::C;
+  using Item = typename Traits<R>::Item;
+  const Geom &g = p->g;
+  char *tmp = p->ws + p->off_temp;
+  C *grid = reinterpret_cast<C *>(tmp + p->c_grid);
+  R *acc = reinterpret_cast<R *>(tmp + p->c_img);
+  C *cvis = reinterpret_cast<C *>(tmp + p->c_cvis);
+  uint32_t *counters = p->at<uint32_t>(p->off_counters);
+  const Item *items = p->at<Item>(p->off_items);
+  const Chunk *chunks = p->at<Chunk>(p->off_chunks);
+  const uint32_t *chunk_off = p->at<uint32_t>(p->off_chunk_off);
+  const R *corr = p->at<R>(p->off_corr);
+  GB_CUDA(cudaMemsetAsync(counters, 0, 4 * (size_t)p->nbatches, s));
+  if (sumwt) GB_CUDA(cudaMemsetAsync(sumwt, 0, sizeof(double) * NP, s));
+  const unsigned item_blocks = (unsigned)std::min<int64_t>(
+      ((int64_t)g.nitems + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
+  k_prep_vis<R, NP><<<item_blocks, kThreads, 0, s>>>(
+      g, items, reinterpret_cast<const C *>(vis), npv, reinterpret_cast<const R *>(wgt), flags,
+      ftype, pm, psf, cvis, sumwt);
+  GB_LAUNCH_CHECK("k_prep_vis");
+  const size_t plane = (size_t)g.ngx * g.ngy;
+  const int64_t npix = (int64_t)g.nx * g.ny;
+  const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
+                                                          (int64_t)p->num_sms * 32);
+  const size_t smem = tile_smem_bytes(p);
+  for (int bi = 0; bi < p->nbatches; ++bi) {
+    const int b0 = bi * g.B;
+    const int nb = std::min(g.B, g.nplanes - b0);
+    GB_CUDA(cudaMemsetAsync(grid, 0, sizeof(C) * (size_t)nb * NP * plane, s));
+    k_grid<R, NP><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks, chunk_off, b0,
+                                                         nb, grid, counters + bi);
+    GB_LAUNCH_CHECK("k_grid");
+    int rc = run_fft(p, nb, grid, CUFFT_INVERSE, s);
+    if (rc) return rc;
+    k_screen_acc<R, NP><<<pix_blocks, kThreads, 0, s>>>(g, grid, b0, nb, acc, bi == 0);
+    GB_LAUNCH_CHECK("k_screen_acc");
+  }
+  dim3 fb((g.nx + 31) / 32, (g.ny + 31) / 32, NP);
+  k_finalize<R><<<fb, dim3(32, 8), 0, s>>>(g, acc, corr, reinterpret_cast<R *>(dirty), layout);
+  GB_LAUNCH_CHECK("k_finalize");
+  return GB_OK;
+}
+
+int run_ms2dirty(gb_plan *p, const void *vis, int npv, const void *wgt, const void *flags,
+                 int ftype, const PolMat &pm, int psf, void *dirty, int layout, double *sumwt,
+                 cudaStream_t s) {
+#define GB_CASE(R, NP)                                                                   \
+  return ms2dirty_impl<R, NP>(p, vis, npv, wgt, flags, ftype, pm, psf, dirty, layout, sumwt, \
+                              s)
+  if (p->precision == GB_FP64) {
+    switch (p->g.NP) {
+      case 1: GB_CASE(double, 1);
+      case 2: GB_CASE(double, 2);
+      default: GB_CASE(double, 4);
+    }
+  }
+  switch (p->g.NP) {
+    case 1: GB_CASE(float, 1);
+    case 2: GB_CASE(float, 2);
+    default: GB_CASE(float, 4);
+  }
+#undef GB_CASE
+}
+
+template <typename R, int NP>
+static int setup_grid_impl(gb_plan *p) {
+  const size_t smem = tile_smem_bytes(p);
+  GB_CUDA(cudaFuncSetAttribute(k_grid<R, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+  int per_sm = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid<R, NP>, kThreads, smem));
+  if (per_sm < 1) {
+    set_error("k_grid cannot launch with %zu bytes of shared memory", smem);
+    return GB_ERR_INVALID_ARG;
+  }
+  p->grid_blocks = per_sm * p->num_sms;
+  return GB_OK;
+}
+
+int setup_grid_kernels(gb_plan *p) {
+  if (p->precision == GB_FP64) {
+    switch (p->g.NP) {
+      case 1: return setup_grid_impl<double, 1>(p);
+      case 2: return setup_grid_impl<double, 2>(p);
+      default: return setup_grid_impl<double, 4>(p);
+    }
+  }
+  switch (p->g.NP) {
+    case 1: return setup_grid_impl<float, 1>(p);
+    case 2: return setup_grid_impl<float, 2>(p);
+    default: return setup_grid_impl<float, 4>(p);
+  }
+}
+
+}  // namespace gb

@@ -1,0 +1,916 @@
+// Planning and the device-side bucket sort.
+//
+// gb_plan_create  -> w range on the device (one sync), host geometry,
+//                    cuFFT plans (no device memory), workspace layout.
+// gb_plan_bind    -> count items per (w-slab, uv-tile) bucket with
+//                    warp-aggregated atomics, exclusive scan, scatter one
+//                    compact record per item into bucket order, cut the
+//                    buckets into work chunks, build the correction image.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "es_table.h"
+#include "gb_plan.cuh"
+
+namespace gb {
+
+static thread_local char tl_error[512] = "";
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(tl_error, sizeof(tl_error), fmt, ap);
+  va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  set_error("CUDA error %s (%d) in %s", cudaGetErrorString(e), (int)e, what);
+  return GB_ERR_CUDA;
+}
+
+const char *last_error() { return tl_error; }
+
+bool sync_check_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("RASCIL_GB300_SYNC_CHECK");
+    return v && v[0] == '1';
+  }();
+  return on;
+}
+
+// ---------------------------------------------------------------------
+// Host planning
+
+static int good_size(int n) {
+  if (n < 16) n = 16;
+  for (;; ++n) {
+    if (n & 1) continue;
+    int m = n;
+    for (int f : {2, 3, 5, 7})
+      while (m % f == 0) m /= f;
+    if (m == 1) return n;
+  }
+}
+
+int plan_geometry(const gb_plan_params *p, double w_lo, double w_hi, Geom &g) {
+  if (!p) {
+    set_error("params is NULL");
+    return GB_ERR_INVALID_ARG;
+  }
+  if (p->nrows <= 0 || p->nchan <= 0) {
+    set_error("nrows and nchan must be positive (got %lld, %d)", (long long)p->nrows,
+              p->nchan);
+    return GB_ERR_INVALID_ARG;
+  }
+  if (p->npol != 1 && p->npol != 2 && p->npol != 4) {
+    set_error("npol must be 1, 2 or 4 (got %d)", p->npol);
+    return GB_ERR_INVALID_ARG;
+  }
+  if (p->npix_x < 16 || p->npix_y < 16 || (p->npix_x & 1) || (p->npix_y & 1)) {
+    set_error("npix_x and npix_y must be even and >= 16 (got %d, %d)", p->npix_x,
+              p->npix_y);
+    return GB_ERR_INVALID_ARG;
+  }
+  if (!(p->pixsize_x > 0.0) || !(p->pixsize_y > 0.0) || !std::isfinite(p->pixsize_x) ||
+      !std::isfinite(p->pixsize_y)) {
+    set_error("pixel sizes must be positive and finite");
+    return GB_ERR_INVALID_ARG;
+  }
+  if (p->precision != GB_FP32 && p->precision != GB_FP64) {
+    set_error("precision must be GB_FP32 or GB_FP64");
+    return GB_ERR_INVALID_ARG;
+  }
+  if (!(p->epsilon > 0.0) || !(p->epsilon < 1.0)) {
+    set_error("epsilon must be in (0, 1) (got %g)", p->epsilon);
+    return GB_ERR_INVALID_ARG;
+  }
+  if (p->precision == GB_FP32 && p->epsilon < 1e-6) {
+    set_error("epsilon %g is below what the FP32 form can reach (1e-6); use GB_FP64",
+              p->epsilon);
+    return GB_ERR_INVALID_ARG;
+  }
+  if (!std::isfinite(w_lo) || !std::isfinite(w_hi) || w_hi < w_lo) {
+    set_error("invalid w range [%g, %g]", w_lo, w_hi);
+    return GB_ERR_INVALID_ARG;
+  }
+  memset(&g, 0, sizeof(g));
+  const double sigma = p->sigma > 0.0 ? p->sigma : 2.0;
+  const int ndim = p->do_wstacking ? 3 : 2;
+  int W = 0;
+  double beta = 0.0;
+  bool sigma_known = false;
+  for (int i = 0; i < kGbEsTableSize; ++i) {
+    const GbEsEntry &e = kGbEsTable[i];
+    if (std::fabs(e.sigma - sigma) > 1e-9) continue;
+    sigma_known = true;
+    if (p->support > 0) {
+      if (e.support == p->support) {
+        W = e.support;
+        beta = e.beta;
+        break;
+      }
+    } else if (ndim * e.error <= p->epsilon) {
+      W = e.support;
+      beta = e.beta;
+      break;
+    }
+  }
+  if (!sigma_known) {
+    set_error("sigma %g not tabulated (use 1.25, 1.5, 1.75 or 2.0)", sigma);
+    return GB_ERR_INVALID_ARG;
+  }
+  if (W == 0) {
+    if (p->support > 0)
+      set_error("support %d not tabulated (4..16)", p->support);
+    else
+      set_error("epsilon %g not reachable with sigma %g", p->epsilon, sigma);
+    return GB_ERR_INVALID_ARG;
+  }
+  g.nx = p->npix_x;
+  g.ny = p->npix_y;
+  g.dx = p->pixsize_x;
+  g.dy = p->pixsize_y;
+  g.W = W;
+  g.beta = beta;
+  g.sigma = sigma;
+  g.do_w = p->do_wstacking ? 1 : 0;
+  g.ngx = good_size(std::max((int)std::ceil(sigma * p->npix_x), 2 * W));
+  g.ngy = good_size(std::max((int)std::ceil(sigma * p->npix_y), 2 * W));
+  const double xm = 0.5 * p->npix_x * p->pixsize_x;
+  const double ym = 0.5 * p->npix_y * p->pixsize_y;
+  const double r2 = xm * xm + ym * ym;
+  if (!(r2 < 1.0)) {
+    set_error("field of view reaches the horizon (l^2 + m^2 = %g)", r2);
+    return GB_ERR_INVALID_ARG;
+  }
+  if (g.do_w) {
+    const double tmin = -r2 / (1.0 + std::sqrt(1.0 - r2));
+    const double tmax = 0.0;
+    g.tc = 0.5 * (tmin + tmax);
+    const double half = 0.5 * (tmax - tmin);
+    g.dw = 1.0 / (2.0 * sigma * half);
+    g.w_lo = w_lo;
+    g.w_hi = w_hi;
+    const double span = std::ceil((w_hi - w_lo) / g.dw);
+    if (span > 1e6) {
+      set_error("w range needs %g w-planes (> 1e6)", span);
+      return GB_ERR_INVALID_ARG;
+    }
+    g.nplanes = (int)span + W;
+  } else {
+    g.tc = 0.0;
+    g.dw = 1.0;
+    g.w_lo = 0.0;
+    g.w_hi = 0.0;
+    g.nplanes = 1;
+  }
+  int T = p->tile > 0 ? p->tile : (p->precision == GB_FP64 ? 16 : 32);
+  if (T < 4 || T > 128) {
+    set_error("tile %d outside [4, 128]", T);
+    return GB_ERR_INVALID_ARG;
+  }
+  int S = p->slab > 0 ? p->slab : 4;
+  if (S > 128) {
+    set_error("slab %d outside [1, 128]", S);
+    return GB_ERR_INVALID_ARG;
+  }
+  g.T = T;
+  g.S = S;
+  g.ntu = (g.ngx + T - 1) / T;
+  g.ntv = (g.ngy + T - 1) / T;
+  g.nslabs = (g.nplanes + S - 1) / S;
+  g.nbuckets = (int64_t)g.nslabs * g.ntu * g.ntv;
+  if (g.nbuckets >= (int64_t)0xffffffffLL) {
+    set_error("too many buckets (%lld)", (long long)g.nbuckets);
+    return GB_ERR_INVALID_ARG;
+  }
+  const int64_t nitems = p->nrows * (int64_t)p->nchan;
+  if (nitems >= (int64_t)0xffffffffLL) {
+    set_error("nrows * nchan = %lld exceeds 2^32 - 1; split the call", (long long)nitems);
+    return GB_ERR_INVALID_ARG;
+  }
+  g.R = p->nrows;
+  g.C = p->nchan;
+  g.NP = p->npol;
+  g.nitems = (uint32_t)nitems;
+  const int64_t budget =
+      p->grid_budget_bytes > 0 ? p->grid_budget_bytes : (int64_t)32 << 30;
+  const int64_t per_plane =
+      (int64_t)g.NP * g.ngx * g.ngy * (int64_t)cplx_bytes(p->precision);
+  int64_t B = budget / per_plane;
+  if (B < 1) B = 1;
+  if (B > g.nplanes) B = g.nplanes;
+  g.B = (int)B;
+  g.nquad = std::min(kMaxQuad, 2 * W + 16);
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------
+// Scan
+
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kThreads * kScanItems;
+
+__global__ void k_scan_tiles(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+                             int64_t n_in, int64_t n_out, uint32_t *__restrict__ tile_sums) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = (base + i < n_in) ? in[base + i] : 0u;
+    s += v[i];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __shared__ uint32_t wsum[kWarps];
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t t = lane < kWarps ? wsum[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < kWarps; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < kWarps) wsum[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t warp_off = warp ? wsum[warp - 1] : 0u;
+  uint32_t run = warp_off + x - s;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n_out) out[base + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == kThreads - 1) tile_sums[blockIdx.x] = warp_off + x;
+}
+
+__global__ void k_scan_add(uint32_t *__restrict__ out, int64_t n_out,
+                           const uint32_t *__restrict__ offs) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile;
+  const uint32_t add = offs[blockIdx.x];
+  for (int i = threadIdx.x; i < kScanTile; i += kThreads) {
+    if (base + i < n_out) out[base + i] += add;
+  }
+}
+
+size_t scan_tmp_words(int64_t n) {
+  size_t words = 0;
+  int64_t m = n + 1;
+  while (true) {
+    const int64_t tiles = (m + kScanTile - 1) / kScanTile;
+    if (tiles <= 1) break;
+    words += (size_t)tiles + (size_t)(tiles + 1) + 8;
+    m = tiles + 1;  // next level scans `tiles` sums into tiles+1 outputs
+  }
+  return words + 64;
+}
+
+// out[0..n] = exclusive scan of in[0..n-1], out[n] = total.
+int scan_exclusive(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
+                   cudaStream_t s) {
+  const int64_t n_out = n + 1;
+  const int64_t tiles = (n_out + kScanTile - 1) / kScanTile;
+  uint32_t *sums = tmp;
+  k_scan_tiles<<<(unsigned)tiles, kThreads, 0, s>>>(in, out, n, n_out, sums);
+  GB_LAUNCH_CHECK("k_scan_tiles");
+  if (tiles > 1) {
+    uint32_t *sums_scanned = sums + tiles;
+    int rc = scan_exclusive(sums, sums_scanned, tiles, sums_scanned + tiles + 1 + 8, s);
+    if (rc) return rc;
+    k_scan_add<<<(unsigned)tiles, kThreads, 0, s>>>(out, n_out, sums_scanned);
+    GB_LAUNCH_CHECK("k_scan_add");
+  }
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------
+// w range
+
+__global__ void k_wrange(const double *__restrict__ uvw, int64_t nrows,
+                         double *__restrict__ part) {
+  double lo = INFINITY, hi = -INFINITY, bad = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const double u = uvw[3 * r], v = uvw[3 * r + 1], w = uvw[3 * r + 2];
+    if (!isfinite(u) || !isfinite(v) || !isfinite(w)) {
+      bad += 1.0;
+      continue;
+    }
+    lo = fmin(lo, w);
+    hi = fmax(hi, w);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    bad += __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  __shared__ double s_lo[kWarps], s_hi[kWarps], s_bad[kWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_lo[warp] = lo;
+    s_hi[warp] = hi;
+    s_bad[warp] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < kWarps; ++i) {
+      lo = fmin(lo, s_lo[i]);
+      hi = fmax(hi, s_hi[i]);
+      bad += s_bad[i];
+    }
+    part[3 * blockIdx.x] = lo;
+    part[3 * blockIdx.x + 1] = hi;
+    part[3 * blockIdx.x + 2] = bad;
+  }
+}
+
+// ---------------------------------------------------------------------
+// Bucket sort
+
+__global__ void k_count(const Geom g, const double *__restrict__ uvw,
+                        const double *__restrict__ freq, uint32_t *__restrict__ counts,
+                        uint32_t *__restrict__ keys, uint32_t *__restrict__ ranks) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < g.nitems; base += stride) {
+    const uint64_t i = base + threadIdx.x;
+    const bool active = i < g.nitems;
+    uint32_t key = 0xffffffffu;
+    if (active) {
+      Coord o;
+      item_coord(g, uvw, freq, (uint32_t)i, o);
+      key = bucket_of(g, o);
+    }
+    // warp-aggregated increment: one atomic per distinct key in the warp
+    const uint32_t peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    const uint32_t below = __popc(peers & ((1u << lane) - 1u));
+    uint32_t start = 0;
+    if (lane == leader && active) start = atomicAdd(&counts[key], (uint32_t)__popc(peers));
+    start = __shfl_sync(peers, start, leader);
+    if (active) {
+      keys[i] = key;
+      ranks[i] = start + below;
+    }
+  }
+}
+
+template <typename R>
+__global__ void k_scatter(const Geom g, const double *__restrict__ uvw,
+                          const double *__restrict__ freq, const uint32_t *__restrict__ keys,
+                          const uint32_t *__restrict__ ranks,
+                          const uint32_t *__restrict__ offsets,
+                          typename Traits<R>::Item *__restrict__ items) {
+  using Item = typename Traits<R>::Item;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.nitems; i += stride) {
+    Coord o;
+    item_coord(g, uvw, freq, (uint32_t)i, o);
+    const uint32_t pos = offsets[keys[i]] + ranks[i];
+    Item it;
+    it.idx = (uint32_t)i;
+    const uint32_t lu = (uint32_t)(o.p0 % g.T), lv = (uint32_t)(o.q0 % g.T);
+    const uint32_t lk = (uint32_t)(o.k0 % g.S);
+    it.loc = lu | (lv << 8) | (lk << 16);
+    it.du = (R)o.du;
+    it.dv = (R)o.dv;
+    it.dwf = (R)o.dwf;
+    if (g.do_w) {
+      // exp(-2 pi i w tc), phase reduced in FP64 before the sincos
+      double turns = o.w * g.tc;
+      turns -= rint(turns);
+      R s, c;
+      sincos_2pi((R)turns, &s, &c);
+      it.ph.x = c;
+      it.ph.y = -s;
+    } else {
+      it.ph.x = (R)1;
+      it.ph.y = (R)0;
+    }
+    if constexpr (sizeof(R) == 4) it.pad = 0.0f;
+    items[pos] = it;
+  }
+}
+
+__global__ void k_chunk_counts(const uint32_t *__restrict__ offsets, int64_t nbuckets,
+                               uint32_t *__restrict__ ccounts) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbuckets; b += stride) {
+    const uint32_t n = offsets[b + 1] - offsets[b];
+    ccounts[b] = (n + kChunkItems - 1) / kChunkItems;
+  }
+}
+
+__global__ void k_emit_chunks(const uint32_t *__restrict__ offsets,
+                              const uint32_t *__restrict__ chunk_off, int64_t nbuckets,
+                              Chunk *__restrict__ chunks) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbuckets; b += stride) {
+    const uint32_t lo = offsets[b], hi = offsets[b + 1];
+    uint32_t c = chunk_off[b];
+    for (uint32_t s = lo; s < hi; s += kChunkItems, ++c) {
+      Chunk ch;
+      ch.begin = s;
+      ch.end = min(hi, s + (uint32_t)kChunkItems);
+      ch.bucket = (uint32_t)b;
+      ch.pad = 0;
+      chunks[c] = ch;
+    }
+  }
+}
+
+// Correction image [ny][nx]: 1/(phihat_u phihat_v) and, with w-stacking,
+// 1/(phihat_w(dw t') n).  phihat_w by Gauss-Legendre quadrature of the
+// (even) kernel on [0, W/2].
+template <typename R>
+__global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
+                             const double *__restrict__ cv, const double *__restrict__ qx,
+                             const double *__restrict__ qw, R *__restrict__ corr) {
+  const int64_t npix = (int64_t)g.nx * g.ny;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += stride) {
+    const int iy = (int)(i / g.nx), ix = (int)(i - (int64_t)iy * g.nx);
+    double f = cu[ix] * cv[iy];
+    if (g.do_w) {
+      const double t = pixel_nm1(g, ix, iy);
+      const double nu = g.dw * (t - g.tc);
+      double ph = 0.0;
+      for (int q = 0; q < g.nquad; ++q) ph += qw[q] * cos(2.0 * M_PI * qx[q] * nu);
+      f = f / (2.0 * ph * (1.0 + t));
+    }
+    corr[i] = (R)f;
+  }
+}
+
+// Host: Gauss-Legendre nodes on [-1, 1] (Newton on the Legendre recurrence).
+static void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+    double dp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = 0.0;
+      for (int j = 1; j <= n; ++j) {
+        const double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p2) / j;
+      }
+      dp = n * (z * p0 - p1) / (z * z - 1.0);
+      const double dz = p0 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    x[i] = -z;
+    x[n - 1 - i] = z;
+    w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+static double es_host(double x, double beta) {
+  const double t = 1.0 - x * x;
+  return t > 0.0 ? std::exp(beta * (std::sqrt(t) - 1.0)) : 0.0;
+}
+
+// Fills cu[nx], cv[ny] (1/phihat along u, v) and the half-interval
+// quadrature (nodes in cells, weights * kernel) for the w correction.
+static void correction_tables(const Geom &g, std::vector<double> &out) {
+  const int nq = g.nquad;
+  std::vector<double> x2, w2;
+  gauss_legendre(2 * nq, x2, w2);
+  std::vector<double> qx(nq), qw(nq);
+  for (int q = 0; q < nq; ++q) {
+    const double xn = x2[nq + q];  // positive half
+    qx[q] = xn * 0.5 * g.W;
+    qw[q] = w2[nq + q] * 0.5 * g.W * es_host(xn, g.beta);
+  }
+  auto phihat = [&](double nu) {
+    double s = 0.0;
+    for (int q = 0; q < nq; ++q) s += qw[q] * std::cos(2.0 * M_PI * qx[q] * nu);
+    return 2.0 * s;
+  };
+  out.assign((size_t)g.nx + g.ny + 2 * nq, 0.0);
+  for (int i = 0; i < g.nx; ++i) out[i] = 1.0 / phihat((double)(i - g.nx / 2) / g.ngx);
+  for (int j = 0; j < g.ny; ++j)
+    out[g.nx + j] = 1.0 / phihat((double)(j - g.ny / 2) / g.ngy);
+  for (int q = 0; q < nq; ++q) {
+    out[g.nx + g.ny + q] = qx[q];
+    out[g.nx + g.ny + nq + q] = qw[q];
+  }
+}
+
+static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static int make_fft(gb_plan *p, int planes, cufftHandle *h, size_t *work) {
+  const Geom &g = p->g;
+  if (cufftCreate(h) != CUFFT_SUCCESS) {
+    set_error("cufftCreate failed");
+    return GB_ERR_CUFFT;
+  }
+  if (cufftSetAutoAllocation(*h, 0) != CUFFT_SUCCESS) {
+    set_error("cufftSetAutoAllocation failed");
+    return GB_ERR_CUFFT;
+  }
+  long long n[2] = {g.ngy, g.ngx};
+  const long long batch = (long long)planes * g.NP;
+  const cufftType type = p->precision == GB_FP64 ? CUFFT_Z2Z : CUFFT_C2C;
+  const cufftResult r =
+      cufftMakePlanMany64(*h, 2, n, nullptr, 1, 0, nullptr, 1, 0, type, batch, work);
+  if (r != CUFFT_SUCCESS) {
+    set_error("cufftMakePlanMany64 failed (%d) for %lld x %lld x %lld", (int)r, n[0], n[1],
+              batch);
+    return GB_ERR_CUFFT;
+  }
+  return GB_OK;
+}
+
+static int layout_workspace(gb_plan *p) {
+  const Geom &g = p->g;
+  const size_t item_bytes = p->precision == GB_FP64 ? sizeof(ItemD) : sizeof(ItemF);
+  const size_t cb = cplx_bytes(p->precision), rb = real_bytes(p->precision);
+  const int64_t nb1 = g.nbuckets + 1;
+  p->max_chunks = (size_t)g.nitems / kChunkItems +
+                  (size_t)std::min<int64_t>(g.nbuckets, (int64_t)g.nitems) + 1;
+  p->nbatches = (g.nplanes + g.B - 1) / g.B;
+  size_t off = 0;
+  p->off_items = off;
+  off = align_up(off + item_bytes * (size_t)g.nitems);
+  p->off_chunk_off = off;
+  off = align_up(off + 4 * (size_t)nb1);
+  p->off_chunks = off;
+  off = align_up(off + sizeof(Chunk) * p->max_chunks);
+  p->off_corr = off;
+  off = align_up(off + rb * (size_t)g.nx * g.ny);
+  p->off_tables = off;
+  off = align_up(off + 8 * ((size_t)g.nx + g.ny + 2 * kMaxQuad));
+  p->off_counters = off;
+  off = align_up(off + 4 * (size_t)(2 * p->nbatches + 8));
+  p->off_fftwork = off;
+  off = align_up(off + p->fft_work_bytes);
+  p->off_temp = off;
+  // bind temporaries
+  size_t t = 0;
+  p->t_keys = t;
+  t = align_up(t + 4 * (size_t)g.nitems);
+  p->t_ranks = t;
+  t = align_up(t + 4 * (size_t)g.nitems);
+  p->t_counts = t;
+  t = align_up(t + 4 * (size_t)nb1);
+  p->t_offsets = t;
+  t = align_up(t + 4 * (size_t)nb1);
+  p->t_ccounts = t;
+  t = align_up(t + 4 * (size_t)nb1);
+  p->t_scan = t;
+  t = align_up(t + 4 * scan_tmp_words(nb1));
+  const size_t bind_temp = t;
+  // call temporaries
+  size_t c = 0;
+  p->c_grid = c;
+  c = align_up(c + cb * (size_t)g.B * g.NP * g.ngx * (size_t)g.ngy);
+  p->c_img = c;
+  c = align_up(c + rb * (size_t)g.NP * g.nx * (size_t)g.ny);
+  p->c_cvis = c;
+  c = align_up(c + cb * (size_t)g.NP * g.nitems);
+  const size_t call_temp = c;
+  p->ws_bytes = off + std::max(bind_temp, call_temp);
+  return GB_OK;
+}
+
+template <typename R>
+static int run_bind(gb_plan *p, cudaStream_t s) {
+  using Item = typename Traits<R>::Item;
+  const Geom &g = p->g;
+  char *tmp = p->ws + p->off_temp;
+  uint32_t *keys = reinterpret_cast<uint32_t *>(tmp + p->t_keys);
+  uint32_t *ranks = reinterpret_cast<uint32_t *>(tmp + p->t_ranks);
+  uint32_t *counts = reinterpret_cast<uint32_t *>(tmp + p->t_counts);
+  uint32_t *offsets = reinterpret_cast<uint32_t *>(tmp + p->t_offsets);
+  uint32_t *ccounts = reinterpret_cast<uint32_t *>(tmp + p->t_ccounts);
+  uint32_t *stmp = reinterpret_cast<uint32_t *>(tmp + p->t_scan);
+  Item *items = p->at<Item>(p->off_items);
+  uint32_t *chunk_off = p->at<uint32_t>(p->off_chunk_off);
+  Chunk *chunks = p->at<Chunk>(p->off_chunks);
+  const int64_t nb = g.nbuckets;
+  const unsigned item_blocks =
+      (unsigned)std::min<int64_t>(((int64_t)g.nitems + kThreads - 1) / kThreads,
+                                  (int64_t)p->num_sms * 16);
+  const unsigned bucket_blocks = (unsigned)std::min<int64_t>(
+      (nb + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
+  GB_CUDA(cudaMemsetAsync(counts, 0, 4 * (size_t)(nb + 1), s));
+  k_count<<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, counts, keys, ranks);
+  GB_LAUNCH_CHECK("k_count");
+  int rc = scan_exclusive(counts, offsets, nb, stmp, s);
+  if (rc) return rc;
+  k_scatter<R><<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, keys, ranks, offsets,
+                                                 items);
+  GB_LAUNCH_CHECK("k_scatter");
+  k_chunk_counts<<<bucket_blocks, kThreads, 0, s>>>(offsets, nb, ccounts);
+  GB_LAUNCH_CHECK("k_chunk_counts");
+  rc = scan_exclusive(ccounts, chunk_off, nb, stmp, s);
+  if (rc) return rc;
+  k_emit_chunks<<<bucket_blocks, kThreads, 0, s>>>(offsets, chunk_off, nb, chunks);
+  GB_LAUNCH_CHECK("k_emit_chunks");
+  // correction image
+  correction_tables(g, p->host_tables);
+  double *tables = p->at<double>(p->off_tables);
+  GB_CUDA(cudaMemcpyAsync(tables, p->host_tables.data(), 8 * p->host_tables.size(),
+                          cudaMemcpyHostToDevice, s));
+  const double *cu = tables, *cv = tables + g.nx, *qx = tables + g.nx + g.ny,
+               *qw = qx + g.nquad;
+  const int64_t npix = (int64_t)g.nx * g.ny;
+  const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
+                                                          (int64_t)p->num_sms * 32);
+  k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, qx, qw, p->at<R>(p->off_corr));
+  GB_LAUNCH_CHECK("k_corr_image");
+  return GB_OK;
+}
+
+
+// Verification export: per original item, its bucket, first support cell
+// (p0, q0, k0) and offsets (du, dv, dwf) as stored in bucket order.
+template <typename R>
+__global__ void k_export_items(const Geom g, const typename Traits<R>::Item *__restrict__ items,
+                               const Chunk *__restrict__ chunks,
+                               const uint32_t *__restrict__ chunk_off,
+                               uint32_t *__restrict__ bucket_out, int32_t *__restrict__ cell_out,
+                               double *__restrict__ frac_out) {
+  const uint32_t nchunks = chunk_off[g.nbuckets];
+  const int ntiles = g.ntu * g.ntv;
+  for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const Chunk ch = chunks[c];
+    const int slab = (int)(ch.bucket / (uint32_t)ntiles);
+    const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
+    const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
+    for (uint32_t pos = ch.begin + threadIdx.x; pos < ch.end; pos += blockDim.x) {
+      const auto it = items[pos];
+      const uint32_t i = it.idx;
+      if (bucket_out) bucket_out[i] = ch.bucket;
+      if (cell_out) {
+        cell_out[3 * (size_t)i] = tu * g.T + (int)(it.loc & 0xffu);
+        cell_out[3 * (size_t)i + 1] = tv * g.T + (int)((it.loc >> 8) & 0xffu);
+        cell_out[3 * (size_t)i + 2] = slab * g.S + (int)((it.loc >> 16) & 0xffu);
+      }
+      if (frac_out) {
+        frac_out[3 * (size_t)i] = (double)it.du;
+        frac_out[3 * (size_t)i + 1] = (double)it.dv;
+        frac_out[3 * (size_t)i + 2] = (double)it.dwf;
+      }
+    }
+  }
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+const char *gb_last_error_string(void) { return gb::last_error(); }
+
+const char *gb_version(void) { return "rascil_gb300 0.1.0 (sm_103a)"; }
+
+int gb_plan_geometry(const gb_plan_params *params, double w_lo, double w_hi,
+                     gb_plan_info *info) {
+  Geom g;
+  int rc = plan_geometry(params, w_lo, w_hi, g);
+  if (rc) return rc;
+  if (!info) {
+    set_error("info_out is NULL");
+    return GB_ERR_INVALID_ARG;
+  }
+  gb_plan tmp;
+  tmp.g = g;
+  tmp.params = *params;
+  tmp.precision = params->precision;
+  tmp.fft_work_bytes = 0;
+  layout_workspace(&tmp);
+  memset(info, 0, sizeof(*info));
+  info->support = g.W;
+  info->ngrid_x = g.ngx;
+  info->ngrid_y = g.ngy;
+  info->nplanes = g.nplanes;
+  info->planes_per_batch = g.B;
+  info->tile = g.T;
+  info->slab = g.S;
+  info->beta = g.beta;
+  info->sigma = g.sigma;
+  info->dw = g.dw;
+  info->w_lo = g.w_lo;
+  info->w_hi = g.w_hi;
+  info->tc = g.tc;
+  info->nitems = g.nitems;
+  info->nbuckets = g.nbuckets;
+  info->workspace_bytes = (int64_t)tmp.ws_bytes;
+  return GB_OK;
+}
+
+int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
+                   const double *freq_dev, void *stream, gb_plan **plan_out) {
+  if (!params || !uvw_dev || !freq_dev || !plan_out) {
+    set_error("gb_plan_create: NULL argument");
+    return GB_ERR_INVALID_ARG;
+  }
+  *plan_out = nullptr;
+  if (params->nrows <= 0 || params->nchan <= 0) {
+    set_error("nrows and nchan must be positive");
+    return GB_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  // frequencies to the host (validation and the w range)
+  std::vector<double> freq(params->nchan);
+  GB_CUDA(cudaMemcpyAsync(freq.data(), freq_dev, 8 * (size_t)params->nchan,
+                          cudaMemcpyDeviceToHost, s));
+  double w_lo = 0.0, w_hi = 0.0;
+  {
+    const int blocks = 512;
+    double *part = nullptr;
+    GB_CUDA(cudaMallocAsync((void **)&part, 3 * 8 * blocks, s));
+    k_wrange<<<blocks, kThreads, 0, s>>>(uvw_dev, params->nrows, part);
+    cudaError_t le = cudaGetLastError();
+    std::vector<double> hp(3 * blocks);
+    cudaError_t ce = cudaMemcpyAsync(hp.data(), part, 3 * 8 * blocks, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(part, s);
+    if (le != cudaSuccess) return cuda_fail(le, "k_wrange");
+    if (ce != cudaSuccess) return cuda_fail(ce, "w range copy");
+    GB_CUDA(cudaStreamSynchronize(s));
+    double rlo = INFINITY, rhi = -INFINITY, bad = 0.0;
+    for (int b = 0; b < blocks; ++b) {
+      rlo = std::fmin(rlo, hp[3 * b]);
+      rhi = std::fmax(rhi, hp[3 * b + 1]);
+      bad += hp[3 * b + 2];
+    }
+    if (bad > 0.0) {
+      set_error("uvw holds %.0f rows with non-finite values", bad);
+      return GB_ERR_INVALID_ARG;
+    }
+    w_lo = INFINITY;
+    w_hi = -INFINITY;
+    for (int c = 0; c < params->nchan; ++c) {
+      if (!(freq[c] > 0.0) || !std::isfinite(freq[c])) {
+        set_error("frequency %d is not positive and finite (%g)", c, freq[c]);
+        return GB_ERR_INVALID_ARG;
+      }
+      const double sc = freq[c] / kSpeedOfLight;
+      w_lo = std::fmin(w_lo, std::fmin(rlo * sc, rhi * sc));
+      w_hi = std::fmax(w_hi, std::fmax(rlo * sc, rhi * sc));
+    }
+  }
+  gb_plan *p = new gb_plan();
+  p->params = *params;
+  p->precision = params->precision;
+  int rc = plan_geometry(params, w_lo, w_hi, p->g);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  p->uvw = uvw_dev;
+  p->freq = freq_dev;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  // cuFFT plans (host-side; the work area comes from the workspace)
+  size_t w_full = 0, w_rem = 0;
+  rc = make_fft(p, p->g.B, &p->fft_full, &w_full);
+  if (rc) {
+    gb_plan_destroy(p);
+    return rc;
+  }
+  p->fft_full_ok = true;
+  p->rem_planes = p->g.nplanes % p->g.B;
+  if (p->rem_planes) {
+    rc = make_fft(p, p->rem_planes, &p->fft_rem, &w_rem);
+    if (rc) {
+      gb_plan_destroy(p);
+      return rc;
+    }
+    p->fft_rem_ok = true;
+  }
+  // cuFFT refuses a work area that aliases the data, even when it reports
+  // needing none, so the work area always gets a region of its own.
+  p->fft_work_bytes = std::max<size_t>(std::max(w_full, w_rem), 4096);
+  layout_workspace(p);
+  rc = setup_tile_kernels(p);
+  if (rc) {
+    gb_plan_destroy(p);
+    return rc;
+  }
+  *plan_out = p;
+  return GB_OK;
+}
+
+int gb_plan_workspace_size(const gb_plan *plan, size_t *bytes) {
+  if (!plan || !bytes) {
+    set_error("gb_plan_workspace_size: NULL argument");
+    return GB_ERR_INVALID_ARG;
+  }
+  *bytes = plan->ws_bytes;
+  return GB_OK;
+}
+
+int gb_plan_bind(gb_plan *p, void *workspace, size_t bytes, void *stream) {
+  if (!p) {
+    set_error("gb_plan_bind: NULL plan");
+    return GB_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!workspace) {
+    set_error("gb_plan_bind: NULL workspace");
+    return GB_ERR_WORKSPACE;
+  }
+  if (bytes < p->ws_bytes) {
+    set_error("workspace of %zu bytes is smaller than the %zu the plan needs", bytes,
+              p->ws_bytes);
+    return GB_ERR_WORKSPACE;
+  }
+  if (((uintptr_t)workspace) & 255) {
+    set_error("workspace must be 256-byte aligned");
+    return GB_ERR_WORKSPACE;
+  }
+  p->ws = (char *)workspace;
+  const void *fw = p->ws + p->off_fftwork;
+  if (p->fft_full_ok && cufftSetWorkArea(p->fft_full, (void *)fw) != CUFFT_SUCCESS) {
+    set_error("cufftSetWorkArea failed");
+    return GB_ERR_CUFFT;
+  }
+  if (p->fft_rem_ok && cufftSetWorkArea(p->fft_rem, (void *)fw) != CUFFT_SUCCESS) {
+    set_error("cufftSetWorkArea failed");
+    return GB_ERR_CUFFT;
+  }
+  const int rc = p->precision == GB_FP64 ? run_bind<double>(p, s) : run_bind<float>(p, s);
+  if (rc) return rc;
+  p->bound = true;
+  p->last_stream = s;
+  return GB_OK;
+}
+
+int gb_plan_info_get(const gb_plan *p, gb_plan_info *info) {
+  if (!p || !info) {
+    set_error("gb_plan_info_get: NULL argument");
+    return GB_ERR_INVALID_ARG;
+  }
+  const Geom &g = p->g;
+  memset(info, 0, sizeof(*info));
+  info->support = g.W;
+  info->ngrid_x = g.ngx;
+  info->ngrid_y = g.ngy;
+  info->nplanes = g.nplanes;
+  info->planes_per_batch = g.B;
+  info->tile = g.T;
+  info->slab = g.S;
+  info->beta = g.beta;
+  info->sigma = g.sigma;
+  info->dw = g.dw;
+  info->w_lo = g.w_lo;
+  info->w_hi = g.w_hi;
+  info->tc = g.tc;
+  info->nitems = g.nitems;
+  info->nbuckets = g.nbuckets;
+  info->workspace_bytes = (int64_t)p->ws_bytes;
+  return GB_OK;
+}
+
+int gb_plan_export_items(const gb_plan *p, uint32_t *bucket_dev, int32_t *cell_dev,
+                         double *frac_dev, void *stream) {
+  if (!p) {
+    set_error("gb_plan_export_items: NULL plan");
+    return GB_ERR_INVALID_ARG;
+  }
+  if (!p->bound) {
+    set_error("gb_plan_export_items: plan has no workspace (call gb_plan_bind)");
+    return GB_ERR_NOT_BOUND;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned blocks = (unsigned)(p->num_sms * 8);
+  if (p->precision == GB_FP64)
+    k_export_items<double><<<blocks, kThreads, 0, s>>>(
+        p->g, p->at<ItemD>(p->off_items), p->at<Chunk>(p->off_chunks),
+        p->at<uint32_t>(p->off_chunk_off), bucket_dev, cell_dev, frac_dev);
+  else
+    k_export_items<float><<<blocks, kThreads, 0, s>>>(
+        p->g, p->at<ItemF>(p->off_items), p->at<Chunk>(p->off_chunks),
+        p->at<uint32_t>(p->off_chunk_off), bucket_dev, cell_dev, frac_dev);
+  GB_LAUNCH_CHECK("k_export_items");
+  return GB_OK;
+}
+
+int gb_plan_destroy(gb_plan *p) {
+  if (!p) return GB_OK;
+  if (p->last_stream || p->bound) cudaStreamSynchronize(p->last_stream);
+  if (p->fft_full_ok) cufftDestroy(p->fft_full);
+  if (p->fft_rem_ok) cufftDestroy(p->fft_rem);
+  delete p;
+  return GB_OK;
+}
+
+}  // extern "C"

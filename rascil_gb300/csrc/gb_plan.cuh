@@ -1,0 +1,88 @@
+// Plan object and launch helpers shared by gb_plan.cu, gb_invert.cu,
+// gb_predict.cu and gb_capi.cu.
+#pragma once
+
+#include <cufft.h>
+
+#include <string>
+#include <vector>
+
+#include "gb_internal.cuh"
+
+struct gb_plan {
+  gb::Geom g;
+  gb_plan_params params;
+  int precision;              // gb_precision
+  const double *uvw = nullptr;   // caller's device arrays (used by bind)
+  const double *freq = nullptr;
+  // host tables uploaded at bind (kept alive for the async copy)
+  std::vector<double> host_tables;  // cu[nx] | cv[ny] | quad_x[nq] | quad_w[nq]
+  // workspace layout (byte offsets)
+  size_t ws_bytes = 0;
+  char *ws = nullptr;
+  size_t off_items = 0, off_chunk_off = 0, off_chunks = 0, off_corr = 0,
+         off_tables = 0, off_counters = 0, off_fftwork = 0, off_temp = 0;
+  // bind-time temporaries (inside the temp region)
+  size_t t_keys = 0, t_ranks = 0, t_counts = 0, t_offsets = 0, t_ccounts = 0,
+         t_scan = 0;
+  // call-time temporaries (inside the temp region)
+  size_t c_grid = 0, c_img = 0, c_cvis = 0;
+  size_t max_chunks = 0;
+  int nbatches = 0;
+  int rem_planes = 0;
+  cufftHandle fft_full = 0, fft_rem = 0;
+  bool fft_full_ok = false, fft_rem_ok = false;
+  size_t fft_work_bytes = 0;
+  bool bound = false;
+  bool owns_ws = false;
+  cudaStream_t last_stream = nullptr;
+  int num_sms = 0;
+  int grid_blocks = 0, degrid_blocks = 0;  // persistent grid sizes
+
+  template <typename T> T *at(size_t off) const {
+    return reinterpret_cast<T *>(ws + off);
+  }
+};
+
+namespace gb {
+
+// Host planning (no device work).  Returns GB_OK or GB_ERR_INVALID_ARG.
+int plan_geometry(const gb_plan_params *p, double w_lo, double w_hi, Geom &g);
+
+// Sizes of one complex / real element for the plan's precision.
+inline size_t cplx_bytes(int precision) { return precision == GB_FP64 ? 16 : 8; }
+inline size_t real_bytes(int precision) { return precision == GB_FP64 ? 8 : 4; }
+
+// Exclusive scan of n uint32 counts into out[0..n] (out[n] = total).
+int scan_exclusive(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
+                   cudaStream_t s);
+size_t scan_tmp_words(int64_t n);
+
+// Invert / predict drivers (gb_invert.cu / gb_predict.cu).
+int run_ms2dirty(gb_plan *p, const void *vis, int npv, const void *wgt,
+                 const void *flags, int flags_type, const PolMat &pm, int psf,
+                 void *dirty, int layout, double *sumwt, cudaStream_t s);
+int run_dirty2ms(gb_plan *p, const void *dirty, int layout, const void *wgt,
+                 const PolMat &pm, int npv, void *vis, cudaStream_t s);
+int setup_tile_kernels(gb_plan *p);
+
+}  // namespace gb
+
+#define GB_CUDA(call)                                          \
+  do {                                                         \
+    cudaError_t e__ = (call);                                  \
+    if (e__ != cudaSuccess) return gb::cuda_fail(e__, #call);  \
+  } while (0)
+
+// Launch check.  With RASCIL_GB300_SYNC_CHECK=1 in the environment every
+// launch is also synchronised, so an asynchronous fault names its kernel.
+namespace gb {
+bool sync_check_enabled();
+}
+#define GB_LAUNCH_CHECK(what)                                           \
+  do {                                                                  \
+    cudaError_t e__ = cudaGetLastError();                               \
+    if (e__ == cudaSuccess && gb::sync_check_enabled())                 \
+      e__ = cudaDeviceSynchronize();                                    \
+    if (e__ != cudaSuccess) return gb::cuda_fail(e__, what);            \
+  } while (0)
