@@ -167,6 +167,43 @@ int gb_dirty2ms(const double *uvw_dev, const double *freq_dev, int64_t nrows,
                 double pixsize_y, double epsilon, int32_t do_wstacking,
                 int32_t precision, void *ms_dev, void *stream);
 
+/* Component DFT: vis_dev[r][c][p] = sum_k flux[k][c][p] *
+ * exp(-2 pi i (uvw[r] f_c / c) . lmn[k]), lmn rows (l, m, n-1).  Replaces
+ * dft_kernel / dft_gpu_raw_kernel
+ * (rascil/processing_components/imaging/dft.py:123-178, 284-332).
+ *   lmn_dev   [ncomp][3] float64;  flux_dev [ncomp][nchan][npol] complex128
+ *   vis_dev   [nrows][nchan][npol] complex64 (GB_FP32) or complex128 (GB_FP64)
+ *   exact     nonzero: FP64 sincos; zero: FP64 phase, FP32 sincos */
+int gb_dft_components(const double *uvw_dev, const double *freq_dev, int64_t nrows,
+                      int32_t nchan, const double *lmn_dev, const double *flux_dev,
+                      int32_t ncomp, int32_t npol, void *vis_dev, int32_t vis_precision,
+                      int32_t exact, void *stream);
+
+/* Exact dirty-image values at pixels pix_dev [npix][2] (ix, iy) in ducc0's
+ * ms2dirty convention, for polarisation `pol` of ms [nrows][nchan][npol]
+ * (complex64 / complex128 per ms_precision) with optional weights of the
+ * same real precision.  The direct sum the gridder approximates; used as
+ * the oracle at sizes the CPU cannot reach.  No counterpart in the
+ * reference (its tests compare against the DFT of components instead). */
+int gb_dft_pixels(const double *uvw_dev, const double *freq_dev, int64_t nrows,
+                  int32_t nchan, int32_t npol, int32_t pol, const void *ms_dev,
+                  int32_t ms_precision, const void *wgt_dev, const int32_t *pix_dev,
+                  int32_t npix, int32_t npix_x, int32_t npix_y, double pixsize_x,
+                  double pixsize_y, int32_t do_wstacking, int32_t exact, double *out_dev,
+                  void *stream);
+
+/* Kernel profiling (process-wide).  While enabled, every launch of this
+ * library's kernels and cuFFT executions records a CUDA-event pair on its
+ * stream and the algorithmic bytes it must move; gb_profile_get waits for
+ * the recorded events and returns per-kernel totals.  No counterpart in
+ * the reference (its timing is wall-clock around invert_ng, rascil/
+ * processing_components/util/performance.py:40-296). */
+int gb_profile_enable(int32_t on);
+int gb_profile_reset(void);
+int gb_profile_count(void);
+int gb_profile_get(int32_t index, char *name, int32_t name_len, double *total_ms,
+                   int64_t *launches, double *bytes);
+
 /* Message for the calling thread's last non-GB_OK status. */
 const char *gb_last_error_string(void);
 

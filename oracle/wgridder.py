@@ -170,6 +170,33 @@ class Plan:
             phase = numpy.ones(u.shape, dtype=numpy.complex128)
         return p0, q0, k0, du, dv, dwf, phase
 
+    def coords_lambda(self, u, v, w):
+        """Like :meth:`coords` for per-item u, v, w already in wavelengths."""
+        W = self.W
+        fu = u * self.dx
+        fu = fu - numpy.floor(fu)
+        U = fu * self.ngx
+        p0 = numpy.ceil(U - 0.5 * W)
+        du = U - p0
+        fv = v * self.dy
+        fv = fv - numpy.floor(fv)
+        V = fv * self.ngy
+        q0 = numpy.ceil(V - 0.5 * W)
+        dv = V - q0
+        p0 = numpy.mod(p0.astype(numpy.int64), self.ngx)
+        q0 = numpy.mod(q0.astype(numpy.int64), self.ngy)
+        if self.do_w:
+            a = (w - self.w_lo) / self.dw
+            k0 = numpy.ceil(a)
+            dwf = a - k0 + 0.5 * W
+            k0 = numpy.clip(k0.astype(numpy.int64), 0, self.nplanes - W)
+            phase = numpy.exp(-2j * numpy.pi * w * self.tc)
+        else:
+            k0 = numpy.zeros(u.shape, dtype=numpy.int64)
+            dwf = numpy.zeros(u.shape)
+            phase = numpy.ones(u.shape, dtype=numpy.complex128)
+        return p0, q0, k0, du, dv, dwf, phase
+
     def weights(self, du, dv, dwf):
         """Kernel values [n, W] for u, v and (if w-stacking) w."""
         W = self.W

@@ -99,6 +99,16 @@ SIGNATURES = {
     "gb_dirty2ms": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _vp, _vp, _c.c_int32,
                                _c.c_int32, _c.c_double, _c.c_double, _c.c_double,
                                _c.c_int32, _c.c_int32, _vp, _vp]),
+    "gb_dft_components": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _vp, _vp, _c.c_int32,
+                                     _c.c_int32, _vp, _c.c_int32, _c.c_int32, _vp]),
+    "gb_dft_pixels": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32, _c.c_int32, _vp,
+                                 _c.c_int32, _vp, _vp, _c.c_int32, _c.c_int32, _c.c_int32,
+                                 _c.c_double, _c.c_double, _c.c_int32, _c.c_int32, _vp, _vp]),
+    "gb_profile_enable": (_c.c_int, [_c.c_int32]),
+    "gb_profile_reset": (_c.c_int, []),
+    "gb_profile_count": (_c.c_int, []),
+    "gb_profile_get": (_c.c_int, [_c.c_int32, _c.c_char_p, _c.c_int32, _dp,
+                                  _c.POINTER(_c.c_int64), _dp]),
     "gb_last_error_string": (_c.c_char_p, []),
     "gb_version": (_c.c_char_p, []),
 }
@@ -140,3 +150,26 @@ def check(status, what=""):
     if status == GB_ERR_INVALID_ARG:
         raise ValueError(text)
     raise GridderError("status %d: %s" % (status, text))
+
+
+def profile_enable(on=True):
+    load().gb_profile_enable(1 if on else 0)
+
+
+def profile_reset():
+    load().gb_profile_reset()
+
+
+def profile_read():
+    """{kernel: {"ms": total device ms, "launches": n, "bytes": algorithmic bytes}}"""
+    lib = load()
+    out = {}
+    for i in range(lib.gb_profile_count()):
+        name = ctypes.create_string_buffer(64)
+        ms = ctypes.c_double()
+        n = ctypes.c_int64()
+        b = ctypes.c_double()
+        check(lib.gb_profile_get(i, name, 64, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(b)))
+        if n.value:
+            out[name.value.decode()] = {"ms": ms.value, "launches": n.value, "bytes": b.value}
+    return out

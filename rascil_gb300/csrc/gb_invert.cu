@@ -371,10 +371,16 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
   if (sumwt) GB_CUDA(cudaMemsetAsync(sumwt, 0, sizeof(double) * NP, s));
   const unsigned item_blocks = (unsigned)std::min<int64_t>(
       ((int64_t)g.nitems + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
-  k_prep_vis<R, NP><<<item_blocks, kThreads, 0, s>>>(
-      g, items, reinterpret_cast<const C *>(vis), npv, reinterpret_cast<const R *>(wgt), flags,
-      ftype, pm, psf, cvis, sumwt);
-  GB_LAUNCH_CHECK("k_prep_vis");
+  {
+    const double fb = ftype == GB_FLAGS_I64 ? 8.0 : (ftype == GB_FLAGS_U8 ? 1.0 : 0.0);
+    const double per = sizeof(Item) + (psf ? 0.0 : npv * sizeof(C)) +
+                       (wgt ? NP * sizeof(R) : 0.0) + npv * fb + NP * sizeof(C);
+    ProfScope ps(kProfPrepVis, s, per * (double)g.nitems);
+    k_prep_vis<R, NP><<<item_blocks, kThreads, 0, s>>>(
+        g, items, reinterpret_cast<const C *>(vis), npv, reinterpret_cast<const R *>(wgt), flags,
+        ftype, pm, psf, cvis, sumwt);
+    GB_LAUNCH_CHECK("k_prep_vis");
+  }
   const size_t plane = (size_t)g.ngx * g.ngy;
   const int64_t npix = (int64_t)g.nx * g.ny;
   const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
@@ -383,18 +389,34 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
   for (int bi = 0; bi < p->nbatches; ++bi) {
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
+    const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
     GB_CUDA(cudaMemsetAsync(grid, 0, sizeof(C) * (size_t)nb * NP * plane, s));
-    k_grid<R, NP><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks, chunk_off, b0,
-                                                         nb, grid, counters + bi);
-    GB_LAUNCH_CHECK("k_grid");
-    int rc = run_fft(p, nb, grid, CUFFT_INVERSE, s);
+    {
+      ProfScope ps(kProfGrid, s,
+                   (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) + gbytes);
+      k_grid<R, NP><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks, chunk_off,
+                                                           b0, nb, grid, counters + bi);
+      GB_LAUNCH_CHECK("k_grid");
+    }
+    int rc;
+    {
+      ProfScope ps(kProfFftInv, s, 2.0 * gbytes);
+      rc = run_fft(p, nb, grid, CUFFT_INVERSE, s);
+    }
     if (rc) return rc;
-    k_screen_acc<R, NP><<<pix_blocks, kThreads, 0, s>>>(g, grid, b0, nb, acc, bi == 0);
-    GB_LAUNCH_CHECK("k_screen_acc");
+    {
+      ProfScope ps(kProfScreenAcc, s,
+                   (double)sizeof(C) * nb * NP * npix + (bi ? 2.0 : 1.0) * sizeof(R) * NP * npix);
+      k_screen_acc<R, NP><<<pix_blocks, kThreads, 0, s>>>(g, grid, b0, nb, acc, bi == 0);
+      GB_LAUNCH_CHECK("k_screen_acc");
+    }
   }
   dim3 fb((g.nx + 31) / 32, (g.ny + 31) / 32, NP);
-  k_finalize<R><<<fb, dim3(32, 8), 0, s>>>(g, acc, corr, reinterpret_cast<R *>(dirty), layout);
-  GB_LAUNCH_CHECK("k_finalize");
+  {
+    ProfScope ps(kProfFinalize, s, 3.0 * sizeof(R) * NP * (double)npix);
+    k_finalize<R><<<fb, dim3(32, 8), 0, s>>>(g, acc, corr, reinterpret_cast<R *>(dirty), layout);
+    GB_LAUNCH_CHECK("k_finalize");
+  }
   return GB_OK;
 }
 

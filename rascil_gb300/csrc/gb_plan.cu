@@ -430,6 +430,12 @@ __global__ void k_emit_chunks(const uint32_t *__restrict__ offsets,
   }
 }
 
+__global__ void k_slab_items(const uint32_t *__restrict__ offsets, int nslabs, int64_t ntiles,
+                             uint32_t *__restrict__ out) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s <= nslabs; s += gridDim.x * blockDim.x)
+    out[s] = offsets[(int64_t)s * ntiles];
+}
+
 // Correction image [ny][nx]: 1/(phihat_u phihat_v) and, with w-stacking,
 // 1/(phihat_w(dw t') n).  phihat_w by Gauss-Legendre quadrature of the
 // (even) kernel on [0, W/2].
@@ -607,20 +613,44 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
                                   (int64_t)p->num_sms * 16);
   const unsigned bucket_blocks = (unsigned)std::min<int64_t>(
       (nb + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
+  const double ni = (double)g.nitems, rows = (double)g.R * 24.0 + 8.0 * g.C;
   GB_CUDA(cudaMemsetAsync(counts, 0, 4 * (size_t)(nb + 1), s));
-  k_count<<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, counts, keys, ranks);
-  GB_LAUNCH_CHECK("k_count");
-  int rc = scan_exclusive(counts, offsets, nb, stmp, s);
+  {
+    ProfScope ps(kProfCountKernel, s, rows + 8.0 * ni);
+    k_count<<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, counts, keys, ranks);
+    GB_LAUNCH_CHECK("k_count");
+  }
+  int rc;
+  {
+    ProfScope ps(kProfScan, s, 8.0 * (double)(nb + 1));
+    rc = scan_exclusive(counts, offsets, nb, stmp, s);
+  }
   if (rc) return rc;
-  k_scatter<R><<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, keys, ranks, offsets,
-                                                 items);
-  GB_LAUNCH_CHECK("k_scatter");
-  k_chunk_counts<<<bucket_blocks, kThreads, 0, s>>>(offsets, nb, ccounts);
-  GB_LAUNCH_CHECK("k_chunk_counts");
-  rc = scan_exclusive(ccounts, chunk_off, nb, stmp, s);
-  if (rc) return rc;
-  k_emit_chunks<<<bucket_blocks, kThreads, 0, s>>>(offsets, chunk_off, nb, chunks);
-  GB_LAUNCH_CHECK("k_emit_chunks");
+  {
+    ProfScope ps(kProfScatter, s, rows + ni * (12.0 + sizeof(Item)));
+    k_scatter<R><<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, keys, ranks, offsets,
+                                                   items);
+    GB_LAUNCH_CHECK("k_scatter");
+  }
+  {
+    ProfScope ps(kProfChunks, s, 20.0 * (double)(nb + 1) + 16.0 * ni / kChunkItems);
+    k_chunk_counts<<<bucket_blocks, kThreads, 0, s>>>(offsets, nb, ccounts);
+    GB_LAUNCH_CHECK("k_chunk_counts");
+    rc = scan_exclusive(ccounts, chunk_off, nb, stmp, s);
+    if (rc) return rc;
+    k_emit_chunks<<<bucket_blocks, kThreads, 0, s>>>(offsets, chunk_off, nb, chunks);
+    GB_LAUNCH_CHECK("k_emit_chunks");
+  }
+  // first item of every slab, to the host (one small synchronous copy)
+  {
+    uint32_t *slab_dev = ccounts;  // reuse: ccounts is free after the chunk scan
+    k_slab_items<<<4, kThreads, 0, s>>>(offsets, g.nslabs, (int64_t)g.ntu * g.ntv, slab_dev);
+    GB_LAUNCH_CHECK("k_slab_items");
+    p->slab_items.assign((size_t)g.nslabs + 1, 0u);
+    GB_CUDA(cudaMemcpyAsync(p->slab_items.data(), slab_dev, 4 * ((size_t)g.nslabs + 1),
+                            cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+  }
   // correction image
   correction_tables(g, p->host_tables);
   double *tables = p->at<double>(p->off_tables);
@@ -631,8 +661,11 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   const int64_t npix = (int64_t)g.nx * g.ny;
   const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
                                                           (int64_t)p->num_sms * 32);
-  k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, qx, qw, p->at<R>(p->off_corr));
-  GB_LAUNCH_CHECK("k_corr_image");
+  {
+    ProfScope ps(kProfCorr, s, (double)npix * sizeof(R));
+    k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, qx, qw, p->at<R>(p->off_corr));
+    GB_LAUNCH_CHECK("k_corr_image");
+  }
   return GB_OK;
 }
 
@@ -736,8 +769,12 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
     const int blocks = 512;
     double *part = nullptr;
     GB_CUDA(cudaMallocAsync((void **)&part, 3 * 8 * blocks, s));
-    k_wrange<<<blocks, kThreads, 0, s>>>(uvw_dev, params->nrows, part);
-    cudaError_t le = cudaGetLastError();
+    cudaError_t le;
+    {
+      ProfScope ps(kProfWrange, s, 24.0 * (double)params->nrows);
+      k_wrange<<<blocks, kThreads, 0, s>>>(uvw_dev, params->nrows, part);
+      le = cudaGetLastError();
+    }
     std::vector<double> hp(3 * blocks);
     cudaError_t ce = cudaMemcpyAsync(hp.data(), part, 3 * 8 * blocks, cudaMemcpyDeviceToHost, s);
     cudaFreeAsync(part, s);

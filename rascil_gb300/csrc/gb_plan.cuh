@@ -4,10 +4,12 @@
 
 #include <cufft.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
 #include "gb_internal.cuh"
+#include "gb_profile.cuh"
 
 struct gb_plan {
   gb::Geom g;
@@ -38,6 +40,16 @@ struct gb_plan {
   cudaStream_t last_stream = nullptr;
   int num_sms = 0;
   int grid_blocks = 0, degrid_blocks = 0;  // persistent grid sizes
+  std::vector<uint32_t> slab_items;        // host copy: first item of each slab (+ total)
+
+  // items whose w-slab reaches planes [b0, b0 + nb)
+  uint32_t batch_items(int b0, int nb) const {
+    const int lo = b0 - (g.S + g.W - 2);
+    const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
+    const int s_hi = std::min(g.nslabs - 1, (b0 + nb - 1) / g.S);
+    if (slab_items.empty() || s_lo > s_hi) return 0;
+    return slab_items[s_hi + 1] - slab_items[s_lo];
+  }
 
   template <typename T> T *at(size_t off) const {
     return reinterpret_cast<T *>(ws + off);

@@ -299,9 +299,13 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
   const R *corr = p->at<R>(p->off_corr);
   GB_CUDA(cudaMemsetAsync(counters, 0, 4 * (size_t)p->nbatches, s));
   dim3 fb((g.nx + 31) / 32, (g.ny + 31) / 32, NP);
-  k_prep_image<R><<<fb, dim3(32, 8), 0, s>>>(g, reinterpret_cast<const R *>(dirty), layout, corr,
-                                             img);
-  GB_LAUNCH_CHECK("k_prep_image");
+  const double npix = (double)g.nx * g.ny;
+  {
+    ProfScope ps(kProfPrepImage, s, 3.0 * sizeof(R) * NP * npix);
+    k_prep_image<R><<<fb, dim3(32, 8), 0, s>>>(g, reinterpret_cast<const R *>(dirty), layout,
+                                               corr, img);
+    GB_LAUNCH_CHECK("k_prep_image");
+  }
   const int64_t plane = (int64_t)g.ngx * g.ngy;
   const unsigned cell_blocks = (unsigned)std::min<int64_t>((plane + kThreads - 1) / kThreads,
                                                            (int64_t)p->num_sms * 32);
@@ -309,14 +313,27 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
   for (int bi = 0; bi < p->nbatches; ++bi) {
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
-    k_screen_pad<R, NP><<<cell_blocks, kThreads, 0, s>>>(g, img, b0, nb, grid);
-    GB_LAUNCH_CHECK("k_screen_pad");
-    int rc = run_fft(p, nb, grid, CUFFT_FORWARD, s);
+    const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
+    {
+      ProfScope ps(kProfScreenPad, s, gbytes + sizeof(R) * NP * npix);
+      k_screen_pad<R, NP><<<cell_blocks, kThreads, 0, s>>>(g, img, b0, nb, grid);
+      GB_LAUNCH_CHECK("k_screen_pad");
+    }
+    int rc;
+    {
+      ProfScope ps(kProfFftFwd, s, 2.0 * gbytes);
+      rc = run_fft(p, nb, grid, CUFFT_FORWARD, s);
+    }
     if (rc) return rc;
-    k_degrid<R, NP><<<p->degrid_blocks, kThreads, smem, s>>>(
-        g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
-        reinterpret_cast<const R *>(wgt), pm, counters + bi);
-    GB_LAUNCH_CHECK("k_degrid");
+    {
+      const double nbi = (double)p->batch_items(b0, nb);
+      ProfScope ps(kProfDegrid, s,
+                   nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) + gbytes);
+      k_degrid<R, NP><<<p->degrid_blocks, kThreads, smem, s>>>(
+          g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
+          reinterpret_cast<const R *>(wgt), pm, counters + bi);
+      GB_LAUNCH_CHECK("k_degrid");
+    }
   }
   return GB_OK;
 }

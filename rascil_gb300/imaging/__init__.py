@@ -1,0 +1,3 @@
+"""RASCIL-facing imaging functions backed by the GB300 gridder."""
+from .ng import invert_ng, predict_ng, invert_gb, predict_gb  # noqa: F401
+from .imaging import invert_blockvisibility, predict_blockvisibility  # noqa: F401
