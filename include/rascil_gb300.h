@@ -204,6 +204,25 @@ int gb_profile_count(void);
 int gb_profile_get(int32_t index, char *name, int32_t name_len, double *total_ms,
                    int64_t *launches, double *bytes);
 
+/* Allocation-free w range.  For callers that cannot allocate device memory
+ * where they need it -- a host framework that owns every device buffer, or
+ * a real-time pipeline that forbids allocation after start-up -- this does
+ * the w-range reduction gb_plan_create performs (which takes its scratch
+ * from cudaMallocAsync) with its scratch in a fixed 384 KiB device array
+ * instead, and calls no allocating routine.  No counterpart in the
+ * reference.
+ *   uvw_dev [nrows][3] metres, freq_dev [nchan] Hz (float64, device)
+ *   out_dev [4] float64 (device): w_lo, w_hi in wavelengths over all (row,
+ *           channel) items -- bit-identical to gb_plan_info's w_lo, w_hi --
+ *           then the number of rows with a non-finite coordinate and the
+ *           number of non-positive or non-finite frequencies.
+ * At most 67,108,864 rows per call (GB_ERR_INVALID_ARG beyond).  The first
+ * call on each device looks up the array's device address, so make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race. */
+int gb_wrange_noalloc(const double *uvw_dev, const double *freq_dev, int64_t nrows,
+                      int32_t nchan, double *out_dev, void *stream);
+
 /* Message for the calling thread's last non-GB_OK status. */
 const char *gb_last_error_string(void);
 
