@@ -40,6 +40,7 @@ METRIC = "Mvis/s invert+predict on 1 GB300, FP32 vs FP64 form at rel RMS<=1e-5 v
 SCALES = {
     # name: overrides of the configuration (None = as specified)
     "full": dict(ntimes=None, nchan=None, npixel=None),
+    "medium": dict(ntimes=16, nchan=8, npixel=2048),
     "small": dict(ntimes=8, nchan=4, npixel=2048),
     "tiny": dict(ntimes=2, nchan=2, npixel=512),
 }
@@ -60,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-planes", type=int, default=4,
                     help="w-planes in the CPU baseline sample")
+    ap.add_argument("--grid-budget-gb", type=float, default=0.0,
+                    help="memory for one batch of w-planes (0 = planner default)")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
 
@@ -188,10 +191,13 @@ class Workload:
         torch.cuda.synchronize(device)
 
 
+GRID_BUDGET = [0]
+
+
 def make_plan(wl, precision):
     from rascil_gb300.wgridder import Plan
     return Plan(wl.uvw, wl.freq_dev, wl.npixel, wl.npixel, wl.cell, wl.cell, wl.epsilon, True,
-                npol=wl.npol, precision=precision)
+                npol=wl.npol, precision=precision, grid_budget_bytes=GRID_BUDGET[0])
 
 
 def step(wl, precision, vis, wgt, model):
@@ -447,6 +453,7 @@ def main():
         run_reference(args)
         return
     import torch
+    GRID_BUDGET[0] = int(args.grid_budget_gb * (1 << 30))
     rank, world = dist_setup(args)
     device = torch.device("cuda", torch.cuda.current_device())
     from rascil_gb300 import _lib

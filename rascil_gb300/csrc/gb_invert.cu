@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kThreads)
 template <typename R, int NP>
 __global__ void __launch_bounds__(kThreads)
     k_screen_acc(const Geom g, const typename Traits<R>::C *__restrict__ grid, int b0, int nb,
-                 R *__restrict__ acc, int first) {
+                 const double *__restrict__ tprime, R *__restrict__ acc, int first) {
   using C = typename Traits<R>::C;
   const int64_t npix = (int64_t)g.nx * g.ny;
   const int ox = (g.ngx - g.nx) / 2, oy = (g.ngy - g.ny) / 2;
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kThreads)
     for (int p = 0; p < NP; ++p) a[p] = first ? (R)0 : acc[p * npix + i];
     const size_t gi = (size_t)(iy + oy) * g.ngx + (ix + ox);
     if (g.do_w) {
-      const double tp = pixel_nm1(g, ix, iy) - g.tc;
+      const double tp = tprime[i];
       for (int j = 0; j < nb; ++j) {
         const double turns = plane_turns(g, b0 + j, tp);
         R s, c;
@@ -309,8 +309,8 @@ template <> cufftResult fft_exec<double>(cufftHandle h, void *data, int dir) {
   return cufftExecZ2Z(h, (cufftDoubleComplex *)data, (cufftDoubleComplex *)data, dir);
 }
 
-int run_fft(gb_plan *p, int nb, void *data, int dir, cudaStream_t s) {
-  cufftHandle h = nb == p->g.B ? p->fft_full : p->fft_rem;
+static int fft_one(gb_plan *p, cufftHandle h, void *data, int dir, cudaStream_t s,
+                   const char *what) {
   if (cufftSetStream(h, s) != CUFFT_SUCCESS) {
     set_error("cufftSetStream failed");
     return GB_ERR_CUFFT;
@@ -319,29 +319,18 @@ int run_fft(gb_plan *p, int nb, void *data, int dir, cudaStream_t s) {
                                                 : fft_exec<float>(h, data, dir);
   if (r != CUFFT_SUCCESS) {
     const cudaError_t e = cudaGetLastError();
-    size_t sz = 0;
-    cufftGetSize(h, &sz);
-    // retry through a fresh, self-allocating plan to tell plan from data problems
-    cufftHandle h2;
-    long long n[2] = {p->g.ngy, p->g.ngx};
-    size_t ws2 = 0;
-    cufftCreate(&h2);
-    cufftResult r2 = cufftMakePlanMany64(h2, 2, n, nullptr, 1, 0, nullptr, 1, 0,
-                                         p->precision == GB_FP64 ? CUFFT_Z2Z : CUFFT_C2C,
-                                         (long long)nb * p->g.NP, &ws2);
-    cufftResult r3 = CUFFT_SUCCESS;
-    if (r2 == CUFFT_SUCCESS) {
-      cufftSetStream(h2, s);
-      r3 = p->precision == GB_FP64 ? fft_exec<double>(h2, data, dir)
-                                   : fft_exec<float>(h2, data, dir);
-    }
-    cufftDestroy(h2);
-    set_error("cufftExec failed (cufft status %d, CUDA %s, handle %d, nb %d, B %d, work %zu "
-              "reserved %zu, data %p, ws %p, fresh plan make %d exec %d)",
-              (int)r, cudaGetErrorString(e), (int)h, nb, p->g.B, sz, p->fft_work_bytes, data,
-              (void *)(p->ws + p->off_fftwork), (int)r2, (int)r3);
+    set_error("cufftExec (%s) failed (cufft status %d, CUDA %s)", what, (int)r,
+              cudaGetErrorString(e));
     return GB_ERR_CUFFT;
   }
+  return GB_OK;
+}
+
+// 2-D transform of nb planes x NP pols (in place).
+int run_fft(gb_plan *p, int nb, void *data, int dir, cudaStream_t s) {
+  const cufftHandle h = nb == p->g.B ? p->fft_full : p->fft_rem;
+  const int rc = fft_one(p, h, data, dir, s, dir == CUFFT_INVERSE ? "inverse" : "forward");
+  if (rc) return rc;
   GB_LAUNCH_CHECK("cufftExec");
   return GB_OK;
 }
@@ -407,7 +396,9 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
     {
       ProfScope ps(kProfScreenAcc, s,
                    (double)sizeof(C) * nb * NP * npix + (bi ? 2.0 : 1.0) * sizeof(R) * NP * npix);
-      k_screen_acc<R, NP><<<pix_blocks, kThreads, 0, s>>>(g, grid, b0, nb, acc, bi == 0);
+      k_screen_acc<R, NP><<<pix_blocks, kThreads, 0, s>>>(g, grid, b0, nb,
+                                                           p->at<double>(p->off_tprime), acc,
+                                                           bi == 0);
       GB_LAUNCH_CHECK("k_screen_acc");
     }
   }

@@ -442,7 +442,8 @@ __global__ void k_slab_items(const uint32_t *__restrict__ offsets, int nslabs, i
 template <typename R>
 __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
                              const double *__restrict__ cv, const double *__restrict__ qx,
-                             const double *__restrict__ qw, R *__restrict__ corr) {
+                             const double *__restrict__ qw, R *__restrict__ corr,
+                             double *__restrict__ tprime) {
   const int64_t npix = (int64_t)g.nx * g.ny;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += stride) {
@@ -450,10 +451,16 @@ __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
     double f = cu[ix] * cv[iy];
     if (g.do_w) {
       const double t = pixel_nm1(g, ix, iy);
-      const double nu = g.dw * (t - g.tc);
-      double ph = 0.0;
-      for (int q = 0; q < g.nquad; ++q) ph += qw[q] * cos(2.0 * M_PI * qx[q] * nu);
-      f = f / (2.0 * ph * (1.0 + t));
+      tprime[i] = t - g.tc;
+      // phihat_w(dw t') by quadrature, in the form's own precision
+      const R nu = (R)(g.dw * (t - g.tc));
+      R ph = (R)0;
+      for (int q = 0; q < g.nquad; ++q) {
+        R s, c;
+        sincos_2pi((R)qx[q] * nu, &s, &c);
+        ph += (R)qw[q] * c;
+      }
+      f = f / (2.0 * (double)ph * (1.0 + t));
     }
     corr[i] = (R)f;
   }
@@ -518,8 +525,7 @@ static void correction_tables(const Geom &g, std::vector<double> &out) {
 
 static size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static int make_fft(gb_plan *p, int planes, cufftHandle *h, size_t *work) {
-  const Geom &g = p->g;
+static int fft_create(cufftHandle *h) {
   if (cufftCreate(h) != CUFFT_SUCCESS) {
     set_error("cufftCreate failed");
     return GB_ERR_CUFFT;
@@ -528,6 +534,16 @@ static int make_fft(gb_plan *p, int planes, cufftHandle *h, size_t *work) {
     set_error("cufftSetAutoAllocation failed");
     return GB_ERR_CUFFT;
   }
+  return GB_OK;
+}
+
+// 2-D transforms of `planes` planes x NP pols, batched.  (Pruning the
+// transform to the image's central columns through 1-D strided cuFFT
+// plans measured slower on GB300 than this single batched 2-D plan.)
+static int make_fft_2d(gb_plan *p, int planes, cufftHandle *h, size_t *work) {
+  const Geom &g = p->g;
+  int rc = fft_create(h);
+  if (rc) return rc;
   long long n[2] = {g.ngy, g.ngx};
   const long long batch = (long long)planes * g.NP;
   const cufftType type = p->precision == GB_FP64 ? CUFFT_Z2Z : CUFFT_C2C;
@@ -558,6 +574,8 @@ static int layout_workspace(gb_plan *p) {
   off = align_up(off + sizeof(Chunk) * p->max_chunks);
   p->off_corr = off;
   off = align_up(off + rb * (size_t)g.nx * g.ny);
+  p->off_tprime = off;
+  off = align_up(off + (g.do_w ? 8 * (size_t)g.nx * g.ny : 0));
   p->off_tables = off;
   off = align_up(off + 8 * ((size_t)g.nx + g.ny + 2 * kMaxQuad));
   p->off_counters = off;
@@ -662,8 +680,9 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
                                                           (int64_t)p->num_sms * 32);
   {
-    ProfScope ps(kProfCorr, s, (double)npix * sizeof(R));
-    k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, qx, qw, p->at<R>(p->off_corr));
+    ProfScope ps(kProfCorr, s, (double)npix * (sizeof(R) + (g.do_w ? 8.0 : 0.0)));
+    k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, qx, qw, p->at<R>(p->off_corr),
+                                                     p->at<double>(p->off_tprime));
     GB_LAUNCH_CHECK("k_corr_image");
   }
   return GB_OK;
@@ -818,7 +837,7 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
   cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, dev);
   // cuFFT plans (host-side; the work area comes from the workspace)
   size_t w_full = 0, w_rem = 0;
-  rc = make_fft(p, p->g.B, &p->fft_full, &w_full);
+  rc = make_fft_2d(p, p->g.B, &p->fft_full, &w_full);
   if (rc) {
     gb_plan_destroy(p);
     return rc;
@@ -826,7 +845,7 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
   p->fft_full_ok = true;
   p->rem_planes = p->g.nplanes % p->g.B;
   if (p->rem_planes) {
-    rc = make_fft(p, p->rem_planes, &p->fft_rem, &w_rem);
+    rc = make_fft_2d(p, p->rem_planes, &p->fft_rem, &w_rem);
     if (rc) {
       gb_plan_destroy(p);
       return rc;
@@ -834,7 +853,8 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
     p->fft_rem_ok = true;
   }
   // cuFFT refuses a work area that aliases the data, even when it reports
-  // needing none, so the work area always gets a region of its own.
+  // needing none, so the work area always gets a region of its own.  The
+  // two plans never run concurrently and share it.
   p->fft_work_bytes = std::max<size_t>(std::max(w_full, w_rem), 4096);
   layout_workspace(p);
   rc = setup_tile_kernels(p);
@@ -875,14 +895,14 @@ int gb_plan_bind(gb_plan *p, void *workspace, size_t bytes, void *stream) {
     return GB_ERR_WORKSPACE;
   }
   p->ws = (char *)workspace;
-  const void *fw = p->ws + p->off_fftwork;
-  if (p->fft_full_ok && cufftSetWorkArea(p->fft_full, (void *)fw) != CUFFT_SUCCESS) {
-    set_error("cufftSetWorkArea failed");
-    return GB_ERR_CUFFT;
-  }
-  if (p->fft_rem_ok && cufftSetWorkArea(p->fft_rem, (void *)fw) != CUFFT_SUCCESS) {
-    set_error("cufftSetWorkArea failed");
-    return GB_ERR_CUFFT;
+  void *fw = p->ws + p->off_fftwork;
+  const bool ok[2] = {p->fft_full_ok, p->fft_rem_ok};
+  const cufftHandle hs[2] = {p->fft_full, p->fft_rem};
+  for (int i = 0; i < 2; ++i) {
+    if (ok[i] && cufftSetWorkArea(hs[i], fw) != CUFFT_SUCCESS) {
+      set_error("cufftSetWorkArea failed");
+      return GB_ERR_CUFFT;
+    }
   }
   const int rc = p->precision == GB_FP64 ? run_bind<double>(p, s) : run_bind<float>(p, s);
   if (rc) return rc;

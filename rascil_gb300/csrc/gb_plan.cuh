@@ -32,9 +32,11 @@ struct gb_plan {
   size_t max_chunks = 0;
   int nbatches = 0;
   int rem_planes = 0;
+  // batched 2-D cuFFT plans: full batches of B planes, and the remainder
   cufftHandle fft_full = 0, fft_rem = 0;
   bool fft_full_ok = false, fft_rem_ok = false;
   size_t fft_work_bytes = 0;
+  size_t off_tprime = 0;  // [ny][nx] float64: n - 1 - tc per pixel (w-stacking)
   bool bound = false;
   bool owns_ws = false;
   cudaStream_t last_stream = nullptr;

@@ -53,8 +53,8 @@ __global__ void k_prep_image(const Geom g, const R *__restrict__ dirty, int layo
 
 template <typename R, int NP>
 __global__ void __launch_bounds__(kThreads)
-    k_screen_pad(const Geom g, const R *__restrict__ img, int b0, int nb,
-                 typename Traits<R>::C *__restrict__ grid) {
+    k_screen_pad(const Geom g, const R *__restrict__ img, const double *__restrict__ tprime,
+                 int b0, int nb, typename Traits<R>::C *__restrict__ grid) {
   using C = typename Traits<R>::C;
   const int64_t npix = (int64_t)g.nx * g.ny;
   const int ox = (g.ngx - g.nx) / 2, oy = (g.ngy - g.ny) / 2;
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
       for (int p = 0; p < NP; ++p) v[p] = img[p * npix + pi];
       if (g.do_w) {
-        const double tp = pixel_nm1(g, ix, iy) - g.tc;
+        const double tp = tprime[pi];
         for (int j = 0; j < nb; ++j) {
           const double turns = plane_turns(g, b0 + j, tp);
           R s, c;
@@ -316,7 +316,8 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
     const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
     {
       ProfScope ps(kProfScreenPad, s, gbytes + sizeof(R) * NP * npix);
-      k_screen_pad<R, NP><<<cell_blocks, kThreads, 0, s>>>(g, img, b0, nb, grid);
+      k_screen_pad<R, NP><<<cell_blocks, kThreads, 0, s>>>(g, img, p->at<double>(p->off_tprime),
+                                                           b0, nb, grid);
       GB_LAUNCH_CHECK("k_screen_pad");
     }
     int rc;

@@ -147,7 +147,9 @@ def model_image(cfg, src, phasecentre, freq):
     pol = PolarisationFrame(cfg["image_pol"])
     im = create_image(cfg["npixel"], cfg["cellsize"], phasecentre, frequency=[freq.mean()],
                       channel_bandwidth=[freq.max() - freq.min() + 1.0], polarisation_frame=pol)
-    numpy.add.at(im["pixels"].data[0, 0], (iy, ix), flux)
+    numpy.add.at(im["pixels"].data[0, 0], (numpy.asarray(iy, dtype=numpy.int64),
+                                            numpy.asarray(ix, dtype=numpy.int64)),
+                 numpy.asarray(flux, dtype=numpy.float64))
     return im
 
 

@@ -1,0 +1,167 @@
+"""Host-side logic of the product (CPU only): pol matrices, geometry,
+normalisation, the data-model shim, the planner through the C-ABI (no
+GPU), the symbol table and argument errors."""
+import ctypes
+import os
+import re
+
+import numpy
+import pytest
+
+from tests.cases import rel_rms
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def test_polarisation_matches_reference_golden():
+    from rascil_gb300.polarisation import PolarisationFrame, convert_pol_frame
+    g = numpy.load(os.path.join(GOLDEN, "polarisation.npz"))
+    pairs = sorted({k[3:] for k in g.files if k.startswith("in_")})
+    assert len(pairs) == 13
+    for pair in pairs:
+        a, b = pair.split("_")
+        got = convert_pol_frame(g["in_" + pair], PolarisationFrame(a), PolarisationFrame(b),
+                                polaxis=2)
+        numpy.testing.assert_allclose(got, g["out_" + pair], rtol=0, atol=1e-15, err_msg=pair)
+    for k in g.files:
+        if k.startswith("names_"):
+            assert PolarisationFrame(k[6:]).names == list(g[k])
+
+
+def test_unknown_conversion_raises():
+    from rascil_gb300.polarisation import conversion_matrix
+    with pytest.raises(ValueError):
+        conversion_matrix("linear", "circular")
+
+
+def test_geometry_matches_reference_golden():
+    from rascil_gb300 import simulation as sim
+    g = numpy.load(os.path.join(GOLDEN, "geometry.npz"))
+    x, y, z = sim.enu_to_xyz(g["e"], g["n"], g["u"], float(g["lat"]))
+    numpy.testing.assert_allclose(numpy.stack([x, y, z], -1), g["xyz"], rtol=0, atol=1e-9)
+    uvw = numpy.stack([sim.xyz_to_uvw(g["xyz"], h, float(g["dec"])) for h in g["has"]])
+    numpy.testing.assert_allclose(uvw, g["uvw"], rtol=0, atol=1e-9)
+
+
+def test_baseline_counts_of_named_configurations():
+    from rascil_gb300 import simulation as sim
+    for name, nbl in (("c1", 2016), ("c2", 130816), ("c4", 8128), ("c5", 19306)):
+        uvw, f, pc, cfg = sim.observation(name, ntimes=1)
+        assert uvw.shape == (1, nbl, 3)
+
+
+def test_normalise_sumwt_matches_reference_golden():
+    from rascil_gb300.data_models import Image, WCS
+    from rascil_gb300.imaging.base import normalise_sumwt
+    from rascil_gb300.polarisation import PolarisationFrame
+    g = numpy.load(os.path.join(GOLDEN, "normalise_sumwt.npz"))
+    im = Image(g["image"].copy(), WCS(["RA---SIN", "DEC--SIN", "STOKES", "FREQ"], [5, 5, 1, 1],
+                                      [-1, 1, 1, 1], [0, 0, 1, 1]),
+               PolarisationFrame("stokesI"), None)
+    out = normalise_sumwt(im, g["sumwt"])["pixels"].data
+    numpy.testing.assert_array_equal(out, g["out"])
+
+
+def test_blockvisibility_shim_accessors():
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.data_models import copy_visibility
+    uvw, f, pc, cfg = sim.observation("c1", ntimes=2)
+    b = sim.make_blockvisibility(uvw, f, pc, cfg)
+    b["vis"].data[...] = 1 + 2j
+    b["flags"].data[0, 0, 0, 0] = 1
+    b["imaging_weight"].data[...] = 3.0
+    assert b.blockvisibility_acc.flagged_vis[0, 0, 0, 0] == 0
+    assert b.blockvisibility_acc.flagged_vis[1, 0, 0, 0] == 1 + 2j
+    assert b.blockvisibility_acc.flagged_imaging_weight[0, 0, 0, 0] == 0
+    z = copy_visibility(b, zero=True)
+    assert numpy.all(z["vis"].data == 0) and numpy.all(b["vis"].data == 1 + 2j)
+    assert b.vis.shape == (2, 2016, 1, 1)
+
+
+def test_image_wcs_and_phase_centre():
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.imaging.base import image_is_canonical, image_phasecentre, separation
+    uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
+    im = sim.model_image(cfg, sim.sources(cfg), pc, f)
+    assert image_is_canonical(im)
+    assert separation(image_phasecentre(im), pc) < 1e-15
+    ch = im.image_acc.wcs.sub([4]).wcs_world2pix(f, 0)[0]
+    numpy.testing.assert_allclose(ch, 0.0)
+
+
+def test_phase_rotation_to_offset_image_centre():
+    """shift_vis_to_image multiplies by conj(exp(-2 pi i uvw_lambda.(l, m, n-1)))
+    of the image centre (visibility/base.py:296-357,1248-1264)."""
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.data_models import SkyDirection
+    from rascil_gb300.imaging.base import lmn_of, shift_vis_to_image
+    uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
+    b = sim.make_blockvisibility(uvw, f, pc, cfg)
+    b["vis"].data[...] = 1.0
+    off = SkyDirection(pc.ra.rad + 0.01, pc.dec.rad - 0.005)
+    im = sim.model_image(cfg, sim.sources(cfg), off, f)
+    s = shift_vis_to_image(b, im, tangent=True, inverse=False)
+    l, m, n = lmn_of(off, pc)
+    ph = numpy.exp(2j * numpy.pi * (uvw @ numpy.array([l, m, n - 1.0]))[..., None]
+                   * f / 299792458.0)
+    numpy.testing.assert_allclose(s["vis"].data[..., 0], ph, rtol=0, atol=1e-12)
+    # the inverse (applied to unshifted data, as predict_ng does) is the conjugate
+    inv = shift_vis_to_image(b, im, tangent=True, inverse=True)
+    numpy.testing.assert_allclose(inv["vis"].data[..., 0], numpy.conj(ph), rtol=0, atol=1e-12)
+    # after a shift the phase centres agree and a second shift is a no-op
+    assert shift_vis_to_image(s, im, tangent=True, inverse=True) is s
+
+
+def _header_functions():
+    text = open(os.path.join(ROOT, "include", "rascil_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    from rascil_gb300 import _lib
+    lib = _lib.load()
+    names = _header_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, name
+
+
+@pytest.mark.parametrize("case", [
+    dict(npix_x=63), dict(npol=3), dict(epsilon=1e-8, precision="fp32"),
+    dict(pixsize_x=0.01), dict(sigma=1.9), dict(epsilon=1e-16, precision="fp64")])
+def test_planner_rejects_invalid_arguments(case):
+    from rascil_gb300.wgridder import plan_geometry
+    kw = dict(npix_x=256, npix_y=256, pixsize_x=1e-3, pixsize_y=1e-3, epsilon=1e-5,
+              do_wstacking=True, w_lo=-100.0, w_hi=200.0, precision="fp32", npol=1)
+    kw.update(case)
+    with pytest.raises(ValueError):
+        plan_geometry(**kw)
+
+
+@pytest.mark.parametrize("precision,eps", [("fp64", 1e-12), ("fp32", 1e-5), ("fp64", 1e-7)])
+@pytest.mark.parametrize("do_w", [False, True])
+@pytest.mark.parametrize("npix,cell", [(512, 5e-4), (8192, 1e-5), (250, 2e-3)])
+def test_planner_geometry_matches_oracle(precision, eps, do_w, npix, cell):
+    """The C planner (host only) and the oracle's restatement agree exactly."""
+    from oracle import wgridder as owg
+    from rascil_gb300.wgridder import plan_geometry
+    w_lo, w_hi = -1234.5, 4321.25
+    info = plan_geometry(npix, npix, cell, cell, eps, do_w, w_lo, w_hi, precision=precision)
+    op = owg.Plan(npix, npix, cell, cell, eps, do_w, w_lo, w_hi, fp32=precision == "fp32")
+    assert info["support"] == op.W and info["beta"] == op.beta
+    assert info["ngrid_x"] == op.ngx and info["ngrid_y"] == op.ngy
+    assert info["nplanes"] == op.nplanes
+    if do_w:
+        assert info["dw"] == op.dw and info["tc"] == op.tc
+
+
+def test_es_table_kernel_choice_is_monotone():
+    from oracle.wgridder import es_table
+    rows = es_table()
+    for s in (1.25, 1.5, 1.75, 2.0):
+        errs = [e for (ss, w, b, e) in rows if ss == s]
+        assert len(errs) == 13
+        assert errs[-1] < errs[0] * 1e-6
