@@ -213,6 +213,53 @@ __device__ __forceinline__ double plane_turns(const Geom &g, int k, double tprim
   return ph - rint(ph);
 }
 
+// ---------------------------------------------------------------------
+// Tile kernels: lane map and shared-memory layout.
+//
+// A warp works on one item at a time.  Its lanes form G = 32/AW groups of
+// AW lanes (AW = 8 for W <= 8, 16 for W <= 16); lane (g, a) owns support
+// column a and, depending on NP, either a subset of the polarisations
+// (NP >= G: pols g, g + G, ...) or one polarisation and every RS-th support
+// row (NP < G).  The tile's sub-grid is stored as 2 NP planes (the real
+// parts of every pol, then the imaginary parts) of SW rows x `pitch`
+// words; pitch and the plane stride are chosen so that the lanes of one
+// instruction fall in 32 distinct shared-memory banks.
+
+inline __host__ __device__ int congruent_up(int x, int m) {
+  return x + ((((m % 32) - (x % 32)) % 32) + 32) % 32;
+}
+
+inline __host__ __device__ int group_lanes(int W) { return W <= 8 ? 8 : 16; }
+
+struct TileLayout {
+  int SW, pitch, plane;
+};
+
+inline __host__ __device__ TileLayout tile_layout(int T, int W, int NP) {
+  const int AW = group_lanes(W), G = 32 / AW;
+  const int RS = NP >= G ? 1 : G / NP;
+  TileLayout L;
+  L.SW = T + W - 1;
+  L.pitch = congruent_up(L.SW, AW);
+  L.plane = congruent_up(L.SW * L.pitch, AW * RS);
+  return L;
+}
+
+template <int NP, int AW>
+struct LaneMap {
+  static constexpr int G = 32 / AW;
+  static constexpr int NPL = NP >= G ? NP / G : 1;  // polarisations per lane
+  static constexpr int RS = NP >= G ? 1 : G / NP;   // support-row stride
+  int g, a, p0, r0;
+  __device__ __forceinline__ explicit LaneMap(int lane) {
+    g = lane / AW;
+    a = lane % AW;
+    p0 = NP >= G ? g : g % NP;
+    r0 = NP >= G ? 0 : g / NP;
+  }
+  __device__ __forceinline__ int pol(int i) const { return p0 + i * G; }
+};
+
 // Error reporting -------------------------------------------------------
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);

@@ -126,31 +126,58 @@ __device__ __forceinline__ void batch_slabs(const Geom &g, int b0, int nb, int &
   s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
 }
 
-template <typename R, int NP>
+// Fixed-point accumulation for the shared-memory sub-grid: integer shared
+// atomics are native, floating-point ones are not.  Each chunk gets its own
+// scale (2^30 or 2^61 over the chunk's sum of |value|), so the integer sums
+// can neither overflow nor lose more than one part in 2^30 of that bound.
+template <typename R> struct FixedAcc;
+template <> struct FixedAcc<float> {
+  using T = int;
+  static constexpr double kOne = 1073741824.0;  // 2^30
+};
+template <> struct FixedAcc<double> {
+  using T = long long;
+  static constexpr double kOne = 2305843009213693952.0;  // 2^61
+};
+__device__ __forceinline__ int to_fixed(float v) { return __float2int_rn(v); }
+__device__ __forceinline__ long long to_fixed(double v) { return __double2ll_rn(v); }
+__device__ __forceinline__ void fixed_add(int *p, int v) { atomicAdd(p, v); }
+__device__ __forceinline__ void fixed_add(long long *p, long long v) {
+  atomicAdd(reinterpret_cast<unsigned long long *>(p), static_cast<unsigned long long>(v));
+}
+
+template <typename R, int NP, int AW>
 __global__ void __launch_bounds__(kThreads)
     k_grid(const Geom g, const typename Traits<R>::Item *__restrict__ items,
            const typename Traits<R>::C *__restrict__ cvis, const Chunk *__restrict__ chunks,
            const uint32_t *__restrict__ chunk_off, int b0, int nb,
            typename Traits<R>::C *__restrict__ grid, uint32_t *__restrict__ counter) {
   using C = typename Traits<R>::C;
+  using A = typename FixedAcc<R>::T;
+  using LM = LaneMap<NP, AW>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R *sg = reinterpret_cast<R *>(smem_raw);  // [NP][SW*SW] x (re, im)
-  const int W = g.W, T = g.T, SW = T + W - 1, SW2 = SW * SW;
+  A *acc = reinterpret_cast<A *>(smem_raw);  // [re pols | im pols][SW][pitch]
+  const int W = g.W, T = g.T;
+  const TileLayout L = tile_layout(T, W, NP);
+  const int SW = L.SW, SW2 = SW * SW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const R scale = (R)2 / (R)W;
+  const LM lm(lane);
+  const R scale_u = (R)2 / (R)W;
   const R beta = (R)g.beta;
   const int ntiles = g.ntu * g.ntv;
   const size_t plane = (size_t)g.ngx * g.ngy;
+  const int nrow_steps = (W + LM::RS - 1) / LM::RS;
   int s_lo, s_hi;
   batch_slabs(g, b0, nb, s_lo, s_hi);
   const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
   const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
+  for (int i = threadIdx.x; i < 2 * NP * L.plane; i += kThreads) acc[i] = 0;
   __shared__ uint32_t s_ci;
+  __shared__ double s_red[kWarps];
   for (;;) {
     if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
     __syncthreads();
     const uint32_t ci = s_ci;
-    __syncthreads();
     if (ci >= c_end) break;
     const Chunk ch = chunks[ci];
     const int slab = (int)(ch.bucket / (uint32_t)ntiles);
@@ -161,74 +188,100 @@ __global__ void __launch_bounds__(kThreads)
     const int k_hi = min(min(kbase + g.S + W - 1, g.nplanes), b0 + nb);
     const int n = (int)(ch.end - ch.begin);
     const bool direct = n * W * W < SW2;
+    // chunk scale for the fixed-point sub-grid: 2^k / sum_j max |component|
+    R scale = (R)0, inv = (R)0;
+    if (!direct) {
+      double m = 0.0;
+      for (uint32_t j = ch.begin + threadIdx.x; j < ch.end; j += kThreads) {
+        R mj = (R)0;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const C v = cvis[(size_t)j * NP + p];
+          mj = fmax(mj, fmax(fabs(v.x), fabs(v.y)));
+        }
+        m += (double)mj;
+      }
+      for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+      if (lane == 0) s_red[warp] = m;
+      __syncthreads();
+      double S = 0.0;
+      for (int w = 0; w < kWarps; ++w) S += s_red[w];
+      if (S > 0.0) {
+        scale = (R)(FixedAcc<R>::kOne / S);
+        inv = (R)(S / FixedAcc<R>::kOne);
+      }
+    }
+    __syncthreads();  // s_red and s_ci are reused by the next chunk
     for (int k = k_lo; k < k_hi; ++k) {
       C *gplane = grid + (size_t)(k - b0) * NP * plane;
-      if (!direct) {
-        for (int i = threadIdx.x; i < NP * SW2 * 2; i += kThreads) sg[i] = (R)0;
-        __syncthreads();
-      }
       for (uint32_t j = ch.begin + warp; j < ch.end; j += kWarps) {
         const auto it = items[j];
         const int aw = k - (kbase + (int)((it.loc >> 16) & 0xffu));
         if (aw < 0 || aw >= W) continue;
-        const R fw = g.do_w ? es_kernel(((R)aw - it.dwf) * scale, beta) : (R)1;
-        C c[NP];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          c[p] = cvis[(size_t)j * NP + p];
-          c[p].x *= fw;
-          c[p].y *= fw;
+        const R fw = g.do_w ? es_kernel(((R)aw - it.dwf) * scale_u, beta) : (R)1;
+        // lanes 0..15 hold the u kernel values, 16..31 the v values
+        R kv_lane = (R)0;
+        if (lane < 16) {
+          if (lane < W) kv_lane = es_kernel(((R)lane - it.du) * scale_u, beta);
+        } else if (lane - 16 < W) {
+          kv_lane = es_kernel(((R)(lane - 16) - it.dv) * scale_u, beta);
         }
-        R kl = (R)0;
-        if (lane < W)
-          kl = es_kernel(((R)lane - it.du) * scale, beta);
-        else if (lane >= 16 && lane < 16 + W)
-          kl = es_kernel(((R)(lane - 16) - it.dv) * scale, beta);
+        const R ku = __shfl_sync(0xffffffffu, kv_lane, lm.a);
+        C c[LM::NPL];
+#pragma unroll
+        for (int i = 0; i < LM::NPL; ++i) {
+          c[i] = cvis[(size_t)j * NP + lm.pol(i)];
+          const R f = fw * (direct ? (R)1 : scale);
+          c[i].x *= f;
+          c[i].y *= f;
+        }
         const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
-        const int ncell = W * W;
-        for (int base = 0; base < ncell; base += 32) {
-          const int cell = base + lane;
-          const int b = cell / W, a = cell - b * W;
-          const R ku = __shfl_sync(0xffffffffu, kl, a);
-          const R kv = __shfl_sync(0xffffffffu, kl, 16 + min(b, W - 1));
-          if (cell < ncell) {
+        for (int r = 0; r < nrow_steps; ++r) {
+          const int b = lm.r0 + r * LM::RS;
+          const R kv = __shfl_sync(0xffffffffu, kv_lane, 16 + min(b, W - 1));
+          if (b < W && lm.a < W) {
             const R kk = ku * kv;
             if (direct) {
-              int p = tu * T + lu + a;
+              int p = tu * T + lu + lm.a;
               if (p >= g.ngx) p -= g.ngx;
               int q = tv * T + lv + b;
               if (q >= g.ngy) q -= g.ngy;
-              const R sgn = ((p + q) & 1) ? (R)-1 : (R)1;
-              const R f = sgn * kk;
+              const R f = ((p + q) & 1) ? -kk : kk;
 #pragma unroll
-              for (int pol = 0; pol < NP; ++pol)
-                grid_add(&gplane[pol * plane + (size_t)q * g.ngx + p], f * c[pol].x,
-                         f * c[pol].y);
+              for (int i = 0; i < LM::NPL; ++i)
+                grid_add(&gplane[lm.pol(i) * plane + (size_t)q * g.ngx + p], f * c[i].x,
+                         f * c[i].y);
             } else {
-              const int si = (lv + b) * SW + (lu + a);
+              const int cell = (lv + b) * L.pitch + lu + lm.a;
 #pragma unroll
-              for (int pol = 0; pol < NP; ++pol) {
-                atomicAdd(&sg[2 * (pol * SW2 + si)], kk * c[pol].x);
-                atomicAdd(&sg[2 * (pol * SW2 + si) + 1], kk * c[pol].y);
+              for (int i = 0; i < LM::NPL; ++i) {
+                const int pl = lm.pol(i);
+                fixed_add(&acc[pl * L.plane + cell], to_fixed(kk * c[i].x));
+                fixed_add(&acc[(NP + pl) * L.plane + cell], to_fixed(kk * c[i].y));
               }
             }
           }
         }
       }
-      __syncthreads();
       if (!direct) {
+        __syncthreads();
+        // flush: fixed point -> float, add to HBM, and leave the sub-grid zeroed
         for (int i = threadIdx.x; i < SW2; i += kThreads) {
           const int y = i / SW, x = i - y * SW;
+          const int cell = y * L.pitch + x;
           int p = tu * T + x;
           while (p >= g.ngx) p -= g.ngx;
           int q = tv * T + y;
           while (q >= g.ngy) q -= g.ngy;
-          const R sgn = ((p + q) & 1) ? (R)-1 : (R)1;
+          const R sgn = ((p + q) & 1) ? -inv : inv;
 #pragma unroll
           for (int pol = 0; pol < NP; ++pol) {
-            const R re = sg[2 * (pol * SW2 + i)], im = sg[2 * (pol * SW2 + i) + 1];
-            if (re != (R)0 || im != (R)0)
-              grid_add(&gplane[pol * plane + (size_t)q * g.ngx + p], sgn * re, sgn * im);
+            const A re = acc[pol * L.plane + cell], im = acc[(NP + pol) * L.plane + cell];
+            if (re != 0 || im != 0) {
+              acc[pol * L.plane + cell] = 0;
+              acc[(NP + pol) * L.plane + cell] = 0;
+              grid_add(&gplane[pol * plane + (size_t)q * g.ngx + p], sgn * (R)re, sgn * (R)im);
+            }
           }
         }
         __syncthreads();
@@ -335,9 +388,10 @@ int run_fft(gb_plan *p, int nb, void *data, int dir, cudaStream_t s) {
   return GB_OK;
 }
 
+// Shared memory of k_grid / k_degrid: 2 NP planes of 4- or 8-byte words.
 size_t tile_smem_bytes(const gb_plan *p) {
-  const int SW = p->g.T + p->g.W - 1;
-  return (size_t)p->g.NP * SW * SW * 2 * real_bytes(p->precision);
+  const TileLayout L = tile_layout(p->g.T, p->g.W, p->g.NP);
+  return (size_t)2 * p->g.NP * L.plane * real_bytes(p->precision);
 }
 
 template <typename R, int NP>
@@ -383,8 +437,14 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
     {
       ProfScope ps(kProfGrid, s,
                    (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) + gbytes);
-      k_grid<R, NP><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks, chunk_off,
-                                                           b0, nb, grid, counters + bi);
+      if (group_lanes(g.W) == 8)
+        k_grid<R, NP, 8><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks,
+                                                                chunk_off, b0, nb, grid,
+                                                                counters + bi);
+      else
+        k_grid<R, NP, 16><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks,
+                                                                 chunk_off, b0, nb, grid,
+                                                                 counters + bi);
       GB_LAUNCH_CHECK("k_grid");
     }
     int rc;
@@ -432,19 +492,25 @@ int run_ms2dirty(gb_plan *p, const void *vis, int npv, const void *wgt, const vo
 #undef GB_CASE
 }
 
-template <typename R, int NP>
-static int setup_grid_impl(gb_plan *p) {
+template <typename R, int NP, int AW>
+static int setup_grid_aw(gb_plan *p) {
   const size_t smem = tile_smem_bytes(p);
-  GB_CUDA(cudaFuncSetAttribute(k_grid<R, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  GB_CUDA(cudaFuncSetAttribute(k_grid<R, NP, AW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
   int per_sm = 0;
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid<R, NP>, kThreads, smem));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grid<R, NP, AW>, kThreads,
+                                                        smem));
   if (per_sm < 1) {
     set_error("k_grid cannot launch with %zu bytes of shared memory", smem);
     return GB_ERR_INVALID_ARG;
   }
   p->grid_blocks = per_sm * p->num_sms;
   return GB_OK;
+}
+
+template <typename R, int NP>
+static int setup_grid_impl(gb_plan *p) {
+  return group_lanes(p->g.W) == 8 ? setup_grid_aw<R, NP, 8>(p) : setup_grid_aw<R, NP, 16>(p);
 }
 
 int setup_grid_kernels(gb_plan *p) {

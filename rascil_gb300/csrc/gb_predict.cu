@@ -109,7 +109,7 @@ __device__ __forceinline__ R warp_sum(R x) {
   return x;
 }
 
-template <typename R, int NP>
+template <typename R, int NP, int AW>
 __global__ void __launch_bounds__(kThreads)
     k_degrid(const Geom g, const typename Traits<R>::Item *__restrict__ items,
              const Chunk *__restrict__ chunks, const uint32_t *__restrict__ chunk_off, int b0,
@@ -117,15 +117,20 @@ __global__ void __launch_bounds__(kThreads)
              typename Traits<R>::C *__restrict__ vis, int npv, const R *__restrict__ wgt,
              const PolMat pm, uint32_t *__restrict__ counter) {
   using C = typename Traits<R>::C;
+  using LM = LaneMap<NP, AW>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C *sg = reinterpret_cast<C *>(smem_raw);  // [NP][SW*SW]
-  const int W = g.W, T = g.T, SW = T + W - 1, SW2 = SW * SW;
+  R *sg = reinterpret_cast<R *>(smem_raw);  // [re pols | im pols][SW][pitch]
+  const int W = g.W, T = g.T;
+  const TileLayout L = tile_layout(T, W, NP);
+  const int SW = L.SW, SW2 = SW * SW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const R scale = (R)2 / (R)W;
+  const LM lm(lane);
+  const R scale_u = (R)2 / (R)W;
   const R beta = (R)g.beta;
   const int ntiles = g.ntu * g.ntv;
   const int64_t plane = (int64_t)g.ngx * g.ngy;
   const int wk = g.do_w ? W : 1;
+  const int nrow_steps = (W + LM::RS - 1) / LM::RS;
   const int lo = b0 - (g.S + W - 2);
   const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
   const int s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
@@ -147,7 +152,7 @@ __global__ void __launch_bounds__(kThreads)
     const int k_hi = min(min(kbase + g.S + W - 1, g.nplanes), b0 + nb);
     const int n = (int)(ch.end - ch.begin);
     const bool direct = n * W * W < SW2;
-    R ar[NP], ai[NP];
+    R ar[NP], ai[NP];  // lane i: running sums of item warp*32 + i
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       ar[p] = (R)0;
@@ -156,6 +161,7 @@ __global__ void __launch_bounds__(kThreads)
     for (int k = k_lo; k < k_hi; ++k) {
       const C *gplane = grid + (int64_t)(k - b0) * NP * plane;
       if (!direct) {
+        // stage the sub-grid (checkerboard sign applied), split re / im
         for (int i = threadIdx.x; i < SW2; i += kThreads) {
           const int y = i / SW, x = i - y * SW;
           int p = tu * T + x;
@@ -163,12 +169,12 @@ __global__ void __launch_bounds__(kThreads)
           int q = tv * T + y;
           while (q >= g.ngy) q -= g.ngy;
           const R sgn = ((p + q) & 1) ? (R)-1 : (R)1;
+          const int cell = y * L.pitch + x;
 #pragma unroll
           for (int pol = 0; pol < NP; ++pol) {
-            C v = gplane[pol * plane + (int64_t)q * g.ngx + p];
-            v.x *= sgn;
-            v.y *= sgn;
-            sg[pol * SW2 + i] = v;
+            const C v = gplane[pol * plane + (int64_t)q * g.ngx + p];
+            sg[pol * L.plane + cell] = sgn * v.x;
+            sg[(NP + pol) * L.plane + cell] = sgn * v.y;
           }
         }
         __syncthreads();
@@ -179,57 +185,76 @@ __global__ void __launch_bounds__(kThreads)
         const auto it = items[j];
         const int aw = k - (kbase + (int)((it.loc >> 16) & 0xffu));
         if (aw < 0 || aw >= wk) continue;
-        R kl = (R)0;
-        if (lane < W)
-          kl = es_kernel(((R)lane - it.du) * scale, beta);
-        else if (lane >= 16 && lane < 16 + W)
-          kl = es_kernel(((R)(lane - 16) - it.dv) * scale, beta);
-        const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
-        R sr[NP], si[NP];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          sr[p] = (R)0;
-          si[p] = (R)0;
+        R kv_lane = (R)0;
+        if (lane < 16) {
+          if (lane < W) kv_lane = es_kernel(((R)lane - it.du) * scale_u, beta);
+        } else if (lane - 16 < W) {
+          kv_lane = es_kernel(((R)(lane - 16) - it.dv) * scale_u, beta);
         }
-        const int ncell = W * W;
-        for (int base = 0; base < ncell; base += 32) {
-          const int cell = base + lane;
-          const int b = cell / W, a = cell - b * W;
-          const R ku = __shfl_sync(0xffffffffu, kl, a);
-          const R kv = __shfl_sync(0xffffffffu, kl, 16 + min(b, W - 1));
-          if (cell < ncell) {
-            const R kk = ku * kv;
+        const R ku = __shfl_sync(0xffffffffu, kv_lane, lm.a);
+        const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
+        R sr[LM::NPL], si[LM::NPL];
+#pragma unroll
+        for (int q = 0; q < LM::NPL; ++q) {
+          sr[q] = (R)0;
+          si[q] = (R)0;
+        }
+        for (int r = 0; r < nrow_steps; ++r) {
+          const int b = lm.r0 + r * LM::RS;
+          const R kv = __shfl_sync(0xffffffffu, kv_lane, 16 + min(b, W - 1));
+          if (b < W && lm.a < W) {
             if (direct) {
-              int p = tu * T + lu + a;
+              int p = tu * T + lu + lm.a;
               if (p >= g.ngx) p -= g.ngx;
               int q = tv * T + lv + b;
               if (q >= g.ngy) q -= g.ngy;
-              const R f = ((p + q) & 1) ? -kk : kk;
+              const R f = ((p + q) & 1) ? -kv : kv;
 #pragma unroll
-              for (int pol = 0; pol < NP; ++pol) {
-                const C v = gplane[pol * plane + (int64_t)q * g.ngx + p];
-                sr[pol] += f * v.x;
-                si[pol] += f * v.y;
+              for (int qq = 0; qq < LM::NPL; ++qq) {
+                const C v = gplane[lm.pol(qq) * plane + (int64_t)q * g.ngx + p];
+                sr[qq] += f * v.x;
+                si[qq] += f * v.y;
               }
             } else {
-              const int idx = (lv + b) * SW + (lu + a);
+              const int cell = (lv + b) * L.pitch + lu + lm.a;
 #pragma unroll
-              for (int pol = 0; pol < NP; ++pol) {
-                const C v = sg[pol * SW2 + idx];
-                sr[pol] += kk * v.x;
-                si[pol] += kk * v.y;
+              for (int qq = 0; qq < LM::NPL; ++qq) {
+                sr[qq] += kv * sg[lm.pol(qq) * L.plane + cell];
+                si[qq] += kv * sg[(NP + lm.pol(qq)) * L.plane + cell];
               }
             }
           }
         }
-        const R fw = g.do_w ? es_kernel(((R)aw - it.dwf) * scale, beta) : (R)1;
+        // sum over the support columns (within a group) and, if several
+        // groups share a polarisation, over their row subsets
+#pragma unroll
+        for (int qq = 0; qq < LM::NPL; ++qq) {
+          R xr = sr[qq] * ku, xi = si[qq] * ku;
+#pragma unroll
+          for (int o = 1; o < AW; o <<= 1) {
+            xr += __shfl_xor_sync(0xffffffffu, xr, o);
+            xi += __shfl_xor_sync(0xffffffffu, xi, o);
+          }
+          if (NP < LM::G) {
+#pragma unroll
+            for (int o = AW * NP; o < 32; o <<= 1) {
+              xr += __shfl_xor_sync(0xffffffffu, xr, o);
+              xi += __shfl_xor_sync(0xffffffffu, xi, o);
+            }
+          }
+          sr[qq] = xr;
+          si[qq] = xi;
+        }
+        const R fw = g.do_w ? es_kernel(((R)aw - it.dwf) * scale_u, beta) : (R)1;
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-          const R tr = warp_sum(sr[p]);
-          const R ti = warp_sum(si[p]);
+          const int holder = (p % LM::G) * AW;
+          const int slot = NP >= LM::G ? p / LM::G : 0;
+          const R vr = __shfl_sync(0xffffffffu, sr[slot], holder);
+          const R vi = __shfl_sync(0xffffffffu, si[slot], holder);
           if (lane == i) {
-            ar[p] += fw * tr;
-            ai[p] += fw * ti;
+            ar[p] += fw * vr;
+            ai[p] += fw * vi;
           }
         }
       }
@@ -309,7 +334,7 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
   const int64_t plane = (int64_t)g.ngx * g.ngy;
   const unsigned cell_blocks = (unsigned)std::min<int64_t>((plane + kThreads - 1) / kThreads,
                                                            (int64_t)p->num_sms * 32);
-  const size_t smem = (size_t)g.NP * (g.T + g.W - 1) * (g.T + g.W - 1) * sizeof(C);
+  const size_t smem = tile_smem_bytes(p);
   for (int bi = 0; bi < p->nbatches; ++bi) {
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
@@ -330,9 +355,14 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
       const double nbi = (double)p->batch_items(b0, nb);
       ProfScope ps(kProfDegrid, s,
                    nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) + gbytes);
-      k_degrid<R, NP><<<p->degrid_blocks, kThreads, smem, s>>>(
-          g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
-          reinterpret_cast<const R *>(wgt), pm, counters + bi);
+      if (group_lanes(g.W) == 8)
+        k_degrid<R, NP, 8><<<p->degrid_blocks, kThreads, smem, s>>>(
+            g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
+            reinterpret_cast<const R *>(wgt), pm, counters + bi);
+      else
+        k_degrid<R, NP, 16><<<p->degrid_blocks, kThreads, smem, s>>>(
+            g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
+            reinterpret_cast<const R *>(wgt), pm, counters + bi);
       GB_LAUNCH_CHECK("k_degrid");
     }
   }
@@ -357,20 +387,26 @@ int run_dirty2ms(gb_plan *p, const void *dirty, int layout, const void *wgt, con
 #undef GB_CASE
 }
 
-template <typename R, int NP>
-static int setup_degrid_impl(gb_plan *p) {
+template <typename R, int NP, int AW>
+static int setup_degrid_aw(gb_plan *p) {
   const size_t smem = tile_smem_bytes(p);
-  GB_CUDA(cudaFuncSetAttribute(k_degrid<R, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  GB_CUDA(cudaFuncSetAttribute(k_degrid<R, NP, AW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
   int per_sm = 0;
-  GB_CUDA(
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_degrid<R, NP>, kThreads, smem));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_degrid<R, NP, AW>, kThreads,
+                                                        smem));
   if (per_sm < 1) {
     set_error("k_degrid cannot launch with %zu bytes of shared memory", smem);
     return GB_ERR_INVALID_ARG;
   }
   p->degrid_blocks = per_sm * p->num_sms;
   return GB_OK;
+}
+
+template <typename R, int NP>
+static int setup_degrid_impl(gb_plan *p) {
+  return group_lanes(p->g.W) == 8 ? setup_degrid_aw<R, NP, 8>(p)
+                                  : setup_degrid_aw<R, NP, 16>(p);
 }
 
 int setup_tile_kernels(gb_plan *p) {
