@@ -63,6 +63,8 @@ def parse():
                     help="w-planes in the CPU baseline sample")
     ap.add_argument("--grid-budget-gb", type=float, default=0.0,
                     help="memory for one batch of w-planes (0 = planner default)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the per-shape autotuner (use cached or default plan parameters)")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
 
@@ -194,14 +196,27 @@ class Workload:
 GRID_BUDGET = [0]
 
 
-def make_plan(wl, precision):
+def make_plan(wl, precision, params=None):
     from rascil_gb300.wgridder import Plan
+    params = params or {}
     return Plan(wl.uvw, wl.freq_dev, wl.npixel, wl.npixel, wl.cell, wl.cell, wl.epsilon, True,
-                npol=wl.npol, precision=precision, grid_budget_bytes=GRID_BUDGET[0])
+                npol=wl.npol, precision=precision, grid_budget_bytes=GRID_BUDGET[0],
+                sigma=params.get("sigma", 0.0), tile=params.get("tile", 0),
+                slab=params.get("slab", 0))
 
 
-def step(wl, precision, vis, wgt, model):
-    plan = make_plan(wl, precision)
+def tune(wl, precision, vis, wgt, model):
+    """Per-shape autotuning (untimed): the plan parameters the timed steps
+    then pick up from the tuning cache."""
+    from rascil_gb300 import tuning
+    key = tuning.shape_key(wl.npixel, wl.npixel, wl.cell, wl.npol, precision, wl.epsilon, True,
+                           wl.nrows, wl.nchan)
+    best, timings = tuning.autotune(key, lambda prm: step(wl, precision, vis, wgt, model, prm))
+    return {"key": key, "chosen": best, "candidate_ms": timings}
+
+
+def step(wl, precision, vis, wgt, model, params=None):
+    plan = make_plan(wl, precision, params)
     dirty = plan.ms2dirty(vis, wgt=wgt, polmat=wl.pm_in, layout="yx")
     pred = plan.dirty2ms(model, polmat=wl.pm_out, npol_vis=wl.npv, layout="yx")
     info = plan.info
@@ -460,6 +475,7 @@ def main():
     _lib.load()
     wl = Workload(args.config, args.scale, device)
     sampler = ClockSampler(device.index) if rank == 0 else None
+    tuned = None if args.no_tune else tune(wl, "fp32", wl.vis32, wl.wgt32, wl.model32)
     if world > 1:
         torch.distributed.barrier()
     ms, out, clocks, stats = time_steps(wl, "fp32", wl.vis32, wl.wgt32, wl.model32, args.steps,
@@ -481,8 +497,9 @@ def main():
             "config": workload_config(wl), "clocks": clocks, "roofline": roof,
             "gpu_launches": int(launches / args.steps),
             "accuracy_fp32": acc32,
-            "plan": {k: info[k] for k in ("support", "ngrid_x", "nplanes", "planes_per_batch",
-                                          "tile", "slab", "beta", "dw")},
+            "plan": {k: info[k] for k in ("support", "sigma", "ngrid_x", "nplanes",
+                                          "planes_per_batch", "tile", "slab", "beta", "dw")},
+            "tuning": tuned,
             "kernels": kernels}
     torch.cuda.empty_cache()
     if not args.no_fp64:

@@ -192,6 +192,23 @@ int gb_dft_pixels(const double *uvw_dev, const double *freq_dev, int64_t nrows,
                   double pixsize_y, int32_t do_wstacking, int32_t exact, double *out_dev,
                   void *stream);
 
+/* Per-antenna complex gains (differentiable predict).  No counterpart in
+ * the reference's ng path; RASCIL applies gains in its calibration code
+ * (rascil/processing_components/calibration/operations.py) on the host.
+ *   gains_dev   [nant][nchan] complex128;  ant1_dev/ant2_dev [nrows] int32
+ *   vis/out     [nrows][nchan][npol] complex64 (GB_FP32) or complex128
+ * gb_apply_gains:   out = g[ant1] conj(g[ant2]) vis
+ * gb_gain_gradient: grad_gains += d L / d gains for a real loss L whose
+ *                   gradient with respect to `out` is grad_dev (dL/dRe + i dL/dIm);
+ *                   grad_gains_dev is accumulated, not overwritten. */
+int gb_apply_gains(const void *vis_dev, const double *gains_dev, const int32_t *ant1_dev,
+                   const int32_t *ant2_dev, int64_t nrows, int32_t nchan, int32_t npol,
+                   int32_t precision, void *out_dev, void *stream);
+int gb_gain_gradient(const void *vis_dev, const void *grad_dev, const double *gains_dev,
+                     const int32_t *ant1_dev, const int32_t *ant2_dev, int64_t nrows,
+                     int32_t nchan, int32_t npol, int32_t nant, int32_t precision,
+                     double *grad_gains_dev, void *stream);
+
 /* Kernel profiling (process-wide).  While enabled, every launch of this
  * library's kernels and cuFFT executions records a CUDA-event pair on its
  * stream and the algorithmic bytes it must move; gb_profile_get waits for

@@ -109,6 +109,10 @@ SIGNATURES = {
     "gb_profile_count": (_c.c_int, []),
     "gb_profile_get": (_c.c_int, [_c.c_int32, _c.c_char_p, _c.c_int32, _dp,
                                   _c.POINTER(_c.c_int64), _dp]),
+    "gb_apply_gains": (_c.c_int, [_vp, _vp, _vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32,
+                                  _c.c_int32, _vp, _vp]),
+    "gb_gain_gradient": (_c.c_int, [_vp, _vp, _vp, _vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32,
+                                    _c.c_int32, _c.c_int32, _vp, _vp]),
     "gb_wrange_noalloc": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _vp, _vp]),
     "gb_last_error_string": (_c.c_char_p, []),
     "gb_version": (_c.c_char_p, []),

@@ -17,7 +17,7 @@ import ctypes
 import numpy
 import torch
 
-from . import _lib
+from . import _lib, tuning
 
 _PREC = {"fp32": _lib.GB_FP32, "fp64": _lib.GB_FP64}
 _LAYOUT = {"xy": _lib.GB_LAYOUT_XY, "yx": _lib.GB_LAYOUT_YX}
@@ -72,6 +72,11 @@ class Plan:
         self.npol = int(npol)
         self.nrows, self.nchan = int(uvw.shape[0]), int(freq.shape[0])
         self.npix_x, self.npix_y = int(npix_x), int(npix_y)
+        self.shape_key = tuning.shape_key(npix_x, npix_y, pixsize_x, npol, precision, epsilon,
+                                          do_wstacking, self.nrows, self.nchan)
+        if not sigma and not tile and not slab:
+            chosen = tuning.choose(self.shape_key, npix_x, npix_y, self.nrows, self.nchan)
+            sigma, tile, slab = chosen["sigma"], chosen["tile"], chosen["slab"]
         self._uvw, self._freq = uvw, freq
         p = _lib.PlanParams()
         p.nrows = self.nrows
