@@ -1,0 +1,96 @@
+"""Many independent snapshot solves on one GPU.
+
+RASCIL images a list of visibility blocks by running one invert/predict per
+block through Dask (``rascil/workflows/rsexecute/imaging/imaging_rsexecute.py:
+72-157``).  Here the whole list runs as one device program:
+
+* one plan per snapshot is created up front (its w range and geometry);
+* a fixed pool of workspace slots, each on its own CUDA stream, is reused
+  round-robin, so the small snapshots' sorts, gridding, FFTs and screens
+  overlap instead of running one after another;
+* the complete sequence (bind/sort + invert + predict for every snapshot)
+  can be captured once as a CUDA graph and replayed with a single launch.
+
+Inputs and outputs are preallocated device tensors so a captured graph can
+be replayed on new data written into the same buffers.
+"""
+import torch
+
+from .wgridder import Plan
+
+
+class SnapshotBatch:
+    """:param snapshots: list of dicts with device tensors ``uvw`` [R, 3]
+    float64 (u, w as ng.py flips them), ``freq`` [C] float64, and ``npix``,
+    ``cell``; :param nslots: concurrent workspace slots / streams."""
+
+    def __init__(self, snapshots, epsilon, precision="fp32", nslots=8, do_wstacking=True,
+                 device="cuda", grid_budget_bytes=2 << 30):
+        self.device = torch.device(device)
+        self.precision = precision
+        self.plans = []
+        for sn in snapshots:
+            self.plans.append(Plan(sn["uvw"], sn["freq"], sn["npix"], sn["npix"], sn["cell"],
+                                   sn["cell"], epsilon, do_wstacking, npol=1,
+                                   precision=precision, bind=False,
+                                   grid_budget_bytes=grid_budget_bytes))
+        self.nslots = max(1, min(int(nslots), len(self.plans)))
+        # slot k serves snapshots k, k + nslots, ...; size it for the largest of them
+        need = [0] * self.nslots
+        for i, p in enumerate(self.plans):
+            need[i % self.nslots] = max(need[i % self.nslots], p.workspace_bytes)
+        self.workspaces = [torch.empty(max(n, 256), dtype=torch.uint8, device=self.device)
+                           for n in need]
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(self.nslots)]
+        cdt = self.plans[0].complex_dtype if self.plans else torch.complex64
+        rdt = self.plans[0].real_dtype if self.plans else torch.float32
+        self.dirty = [torch.empty((1, p.npix_y, p.npix_x), dtype=rdt, device=self.device)
+                      for p in self.plans]
+        self.pred = [torch.empty((p.nrows, p.nchan, 1), dtype=cdt, device=self.device)
+                     for p in self.plans]
+        self.graph = None
+
+    @property
+    def nvis(self):
+        return sum(p.nrows * p.nchan for p in self.plans)
+
+    def run(self, vis, models, concurrent=True):
+        """Invert vis[i] into self.dirty[i] and predict models[i] into
+        self.pred[i] for every snapshot, on the current stream's timeline."""
+        main = torch.cuda.current_stream(self.device)
+        streams = self.streams if concurrent else [main] * self.nslots
+        if concurrent:
+            for s in streams:
+                s.wait_stream(main)
+        for i, p in enumerate(self.plans):
+            k = i % self.nslots
+            with torch.cuda.stream(streams[k]):
+                p.bind(self.workspaces[k])
+                p.ms2dirty(vis[i], layout="yx", out=self.dirty[i])
+                p.dirty2ms(models[i], layout="yx", out=self.pred[i])
+        if concurrent:
+            for s in streams:
+                main.wait_stream(s)
+
+    def capture(self, vis, models):
+        """Record run(vis, models) as a CUDA graph; replay() re-runs it."""
+        self.run(vis, models)  # warm-up outside capture (cuFFT, caches)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run(vis, models)
+        self.graph = g
+        self._keep = (vis, models)
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            raise RuntimeError("capture() first")
+        self.graph.replay()
+
+    def close(self):
+        torch.cuda.synchronize(self.device)
+        for p in self.plans:
+            p.close()
+        self.plans = []
+        self.graph = None

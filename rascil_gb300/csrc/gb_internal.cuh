@@ -87,6 +87,15 @@ struct Chunk {
   uint32_t begin, end, bucket, pad;
 };
 
+// Half-interval Gauss-Legendre quadrature of the ES kernel (nodes in cells,
+// weights times kernel values), passed to kernels by value: the kernel's
+// Fourier transform is phihat(nu) = 2 sum_q w_q cos(2 pi x_q nu).
+struct Quad {
+  int n;
+  double x[kMaxQuad];
+  double w[kMaxQuad];
+};
+
 // Polarisation conversion matrix (nout x nin complex, row-major); the
 // identity is flagged so kernels skip the multiply.
 struct PolMat {

@@ -441,9 +441,8 @@ __global__ void k_slab_items(const uint32_t *__restrict__ offsets, int nslabs, i
 // (even) kernel on [0, W/2].
 template <typename R>
 __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
-                             const double *__restrict__ cv, const double *__restrict__ qx,
-                             const double *__restrict__ qw, R *__restrict__ corr,
-                             double *__restrict__ tprime) {
+                             const double *__restrict__ cv, const Quad quad,
+                             R *__restrict__ corr, double *__restrict__ tprime) {
   const int64_t npix = (int64_t)g.nx * g.ny;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += stride) {
@@ -455,10 +454,10 @@ __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
       // phihat_w(dw t') by quadrature, in the form's own precision
       const R nu = (R)(g.dw * (t - g.tc));
       R ph = (R)0;
-      for (int q = 0; q < g.nquad; ++q) {
+      for (int q = 0; q < quad.n; ++q) {
         R s, c;
-        sincos_2pi((R)qx[q] * nu, &s, &c);
-        ph += (R)qw[q] * c;
+        sincos_2pi((R)quad.x[q] * nu, &s, &c);
+        ph += (R)quad.w[q] * c;
       }
       f = f / (2.0 * (double)ph * (1.0 + t));
     }
@@ -496,30 +495,35 @@ static double es_host(double x, double beta) {
   return t > 0.0 ? std::exp(beta * (std::sqrt(t) - 1.0)) : 0.0;
 }
 
-// Fills cu[nx], cv[ny] (1/phihat along u, v) and the half-interval
-// quadrature (nodes in cells, weights * kernel) for the w correction.
-static void correction_tables(const Geom &g, std::vector<double> &out) {
+// Half-interval quadrature of the ES kernel (nodes in cells, weights times
+// kernel values).
+static void make_quadrature(const Geom &g, Quad &q) {
   const int nq = g.nquad;
   std::vector<double> x2, w2;
   gauss_legendre(2 * nq, x2, w2);
-  std::vector<double> qx(nq), qw(nq);
-  for (int q = 0; q < nq; ++q) {
-    const double xn = x2[nq + q];  // positive half
-    qx[q] = xn * 0.5 * g.W;
-    qw[q] = w2[nq + q] * 0.5 * g.W * es_host(xn, g.beta);
+  q.n = nq;
+  for (int i = 0; i < nq; ++i) {
+    const double xn = x2[nq + i];  // positive half
+    q.x[i] = xn * 0.5 * g.W;
+    q.w[i] = w2[nq + i] * 0.5 * g.W * es_host(xn, g.beta);
   }
-  auto phihat = [&](double nu) {
+}
+
+// cu[ix] = 1/phihat((ix - nx/2)/ngx) and cv[iy] likewise, FP64 on the device
+// (keeps the plan's bind free of host copies, so it can be graph-captured).
+__global__ void k_corr_1d(const Geom g, const Quad quad, double *__restrict__ cu,
+                          double *__restrict__ cv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.nx + g.ny;
+       i += gridDim.x * blockDim.x) {
+    const double nu = i < g.nx ? (double)(i - g.nx / 2) / g.ngx
+                               : (double)(i - g.nx - g.ny / 2) / g.ngy;
     double s = 0.0;
-    for (int q = 0; q < nq; ++q) s += qw[q] * std::cos(2.0 * M_PI * qx[q] * nu);
-    return 2.0 * s;
-  };
-  out.assign((size_t)g.nx + g.ny + 2 * nq, 0.0);
-  for (int i = 0; i < g.nx; ++i) out[i] = 1.0 / phihat((double)(i - g.nx / 2) / g.ngx);
-  for (int j = 0; j < g.ny; ++j)
-    out[g.nx + j] = 1.0 / phihat((double)(j - g.ny / 2) / g.ngy);
-  for (int q = 0; q < nq; ++q) {
-    out[g.nx + g.ny + q] = qx[q];
-    out[g.nx + g.ny + nq + q] = qw[q];
+    for (int q = 0; q < quad.n; ++q) s += quad.w[q] * cos(2.0 * M_PI * quad.x[q] * nu);
+    const double f = 1.0 / (2.0 * s);
+    if (i < g.nx)
+      cu[i] = f;
+    else
+      cv[i - g.nx] = f;
   }
 }
 
@@ -659,8 +663,9 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
     k_emit_chunks<<<bucket_blocks, kThreads, 0, s>>>(offsets, chunk_off, nb, chunks);
     GB_LAUNCH_CHECK("k_emit_chunks");
   }
-  // first item of every slab, to the host (one small synchronous copy)
-  {
+  // first item of every slab, to the host: only the profiler's byte counts
+  // use it, and it costs a synchronisation, so only while profiling is on
+  if (prof_on()) {
     uint32_t *slab_dev = ccounts;  // reuse: ccounts is free after the chunk scan
     k_slab_items<<<4, kThreads, 0, s>>>(offsets, g.nslabs, (int64_t)g.ntu * g.ntv, slab_dev);
     GB_LAUNCH_CHECK("k_slab_items");
@@ -669,19 +674,17 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
                             cudaMemcpyDeviceToHost, s));
     GB_CUDA(cudaStreamSynchronize(s));
   }
-  // correction image
-  correction_tables(g, p->host_tables);
+  // correction factors
   double *tables = p->at<double>(p->off_tables);
-  GB_CUDA(cudaMemcpyAsync(tables, p->host_tables.data(), 8 * p->host_tables.size(),
-                          cudaMemcpyHostToDevice, s));
-  const double *cu = tables, *cv = tables + g.nx, *qx = tables + g.nx + g.ny,
-               *qw = qx + g.nquad;
+  double *cu = tables, *cv = tables + g.nx;
+  k_corr_1d<<<(g.nx + g.ny + kThreads - 1) / kThreads, kThreads, 0, s>>>(g, p->quad, cu, cv);
+  GB_LAUNCH_CHECK("k_corr_1d");
   const int64_t npix = (int64_t)g.nx * g.ny;
   const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
                                                           (int64_t)p->num_sms * 32);
   {
     ProfScope ps(kProfCorr, s, (double)npix * (sizeof(R) + (g.do_w ? 8.0 : 0.0)));
-    k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, qx, qw, p->at<R>(p->off_corr),
+    k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, p->quad, p->at<R>(p->off_corr),
                                                      p->at<double>(p->off_tprime));
     GB_LAUNCH_CHECK("k_corr_image");
   }
@@ -832,6 +835,7 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
   }
   p->uvw = uvw_dev;
   p->freq = freq_dev;
+  make_quadrature(p->g, p->quad);
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, dev);

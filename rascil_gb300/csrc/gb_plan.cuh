@@ -17,8 +17,7 @@ struct gb_plan {
   int precision;              // gb_precision
   const double *uvw = nullptr;   // caller's device arrays (used by bind)
   const double *freq = nullptr;
-  // host tables uploaded at bind (kept alive for the async copy)
-  std::vector<double> host_tables;  // cu[nx] | cv[ny] | quad_x[nq] | quad_w[nq]
+  gb::Quad quad;  // ES-kernel quadrature for the correction factors
   // workspace layout (byte offsets)
   size_t ws_bytes = 0;
   char *ws = nullptr;

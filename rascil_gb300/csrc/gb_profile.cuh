@@ -28,6 +28,9 @@ enum ProfId {
 
 extern const char *kProfNames[kProfCount];
 
+// True while process-wide profiling is enabled.
+bool prof_on();
+
 // Records an event pair around its lifetime on stream `s` when profiling
 // is on; `bytes` is the algorithmic traffic of the enclosed launch.
 class ProfScope {

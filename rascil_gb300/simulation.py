@@ -181,3 +181,40 @@ def make_blockvisibility(uvw, freq, phasecentre, cfg, vis=None):
         dt = numpy.complex128 if cfg["dtype"] == "c16" else numpy.complex64
         vis = numpy.zeros((nt, nbl, len(freq), pol.npol), dtype=dt)
     return BlockVisibility(vis, uvw, freq, phasecentre, pol)
+
+
+def snapshot_batch(nsnap=256, seed=0, min_vis=5000, max_vis=2_000_000,
+                   sizes=(256, 512, 1024, 2048)):
+    """Independent snapshots with uneven shapes (the batched configuration):
+    each draws its own antenna count (32-512, positions uniform in a 1 km
+    disk, latitude -26.7 deg, dec -45 deg), 1-8 channels inside 100-200 MHz,
+    1-16 hour angles, an image side from ``sizes`` and a cell of
+    1/(2.2 max|uv|); the visibility count is kept within [min_vis, max_vis]
+    by trimming antennas.  Returns a list of dicts with uvw [ntimes, nbl, 3]
+    (metres), freq, npix, cell."""
+    rng = numpy.random.default_rng(seed + 77)
+    out = []
+    lat, dec = numpy.radians(-26.7), numpy.radians(-45.0)
+    for s in range(nsnap):
+        nant = int(rng.integers(32, 513))
+        nchan = int(rng.integers(1, 9))
+        ntimes = int(rng.integers(1, 17))
+        while nant > 8 and nant * (nant - 1) // 2 * nchan * ntimes > max_vis:
+            nant = int(nant * 0.9)
+        while nant * (nant - 1) // 2 * nchan * ntimes < min_vis:
+            ntimes += 1
+        e, n = disk_positions(rng, nant, 1000.0)
+        f_lo = rng.uniform(100e6, 190e6)
+        f_hi = min(200e6, f_lo + rng.uniform(1e6, 50e6))
+        freq = numpy.linspace(f_lo, f_hi, nchan) if nchan > 1 else numpy.array([f_lo])
+        h0 = rng.uniform(-3.0, 2.0)
+        ha = numpy.linspace(h0, h0 + rng.uniform(0.0, 1.0), ntimes) * numpy.pi / 12.0
+        uvw = baseline_uvw(e, n, lat, ha, dec)
+        uvmax = numpy.max(numpy.hypot(uvw[..., 0], uvw[..., 1])) * freq.max() / SPEED_OF_LIGHT
+        npix = int(rng.choice(sizes))
+        # 1/(2.2 max|uv|), but never past 0.6 rad from the centre (short
+        # snapshots with large images would otherwise image beyond the horizon)
+        cell = min(1.0 / (2.2 * uvmax), 0.6 / (npix / 2))
+        out.append(dict(uvw=uvw, freq=freq, npix=npix, cell=cell,
+                        nvis=uvw.shape[0] * uvw.shape[1] * nchan))
+    return out

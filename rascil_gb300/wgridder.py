@@ -53,11 +53,13 @@ class Plan:
     :param freq: [nchan] float64 CUDA tensor (Hz)
     :param npol: image polarisations gridded together (1, 2, 4)
     :param precision: "fp32" (complex64 data) or "fp64" (complex128 data)
+    :param bind: allocate a workspace (torch) and run the bucket sort now; with
+        ``bind=False`` call :meth:`bind` with a caller-owned buffer later
     """
 
     def __init__(self, uvw, freq, npix_x, npix_y, pixsize_x, pixsize_y, epsilon,
                  do_wstacking, npol=1, precision="fp32", sigma=0.0, support=0, tile=0,
-                 slab=0, grid_budget_bytes=0):
+                 slab=0, grid_budget_bytes=0, bind=True):
         lib = _lib.load()
         _require_cuda(uvw, "uvw")
         _require_cuda(freq, "freq")
@@ -103,11 +105,27 @@ class Plan:
             self._handle = handle
             size = ctypes.c_size_t()
             _lib.check(lib.gb_plan_workspace_size(handle, ctypes.byref(size)))
-            self.workspace = torch.empty(max(int(size.value), 256), dtype=torch.uint8,
-                                         device=self.device)
-            _lib.check(lib.gb_plan_bind(handle, _ptr(self.workspace), size.value,
-                                        _stream(self.device)), "gb_plan_bind")
+            self.workspace_bytes = int(size.value)
+            self.workspace = None
+            if bind:
+                self.bind(torch.empty(max(self.workspace_bytes, 256), dtype=torch.uint8,
+                                      device=self.device))
         self.info = self._info()
+
+    def bind(self, workspace):
+        """Bind device scratch (a uint8 CUDA tensor of at least
+        ``workspace_bytes``) and run the bucket sort, on the current stream.
+        A plan can be re-bound to another (or the same) buffer at any time;
+        the buffer must stay alive while work that uses it runs."""
+        _require_cuda(workspace, "workspace")
+        if workspace.numel() < self.workspace_bytes:
+            raise ValueError("workspace holds %d bytes, the plan needs %d"
+                             % (workspace.numel(), self.workspace_bytes))
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().gb_plan_bind(self._handle, _ptr(workspace),
+                                                workspace.numel(), _stream(self.device)),
+                       "gb_plan_bind")
+        self.workspace = workspace
 
     def _info(self):
         info = _lib.PlanInfo()
