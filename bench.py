@@ -65,6 +65,9 @@ def parse():
                     help="memory for one batch of w-planes (0 = planner default)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the per-shape autotuner (use cached or default plan parameters)")
+    ap.add_argument("--fft-mode", default="auto", choices=["auto", "columns", "cufft2d"],
+                    help="per-plane transforms of the FP32 form (auto: column kernels where "
+                         "they apply)")
     ap.add_argument("--json-out", default=None)
     return ap.parse_args()
 
@@ -194,6 +197,7 @@ class Workload:
 
 
 GRID_BUDGET = [0]
+FFT_MODE = ["auto"]
 
 
 def make_plan(wl, precision, params=None):
@@ -202,7 +206,7 @@ def make_plan(wl, precision, params=None):
     return Plan(wl.uvw, wl.freq_dev, wl.npixel, wl.npixel, wl.cell, wl.cell, wl.epsilon, True,
                 npol=wl.npol, precision=precision, grid_budget_bytes=GRID_BUDGET[0],
                 sigma=params.get("sigma", 0.0), tile=params.get("tile", 0),
-                slab=params.get("slab", 0))
+                slab=params.get("slab", 0), fft_mode=FFT_MODE[0])
 
 
 def tune(wl, precision, vis, wgt, model):
@@ -469,6 +473,7 @@ def main():
         return
     import torch
     GRID_BUDGET[0] = int(args.grid_budget_gb * (1 << 30))
+    FFT_MODE[0] = args.fft_mode
     rank, world = dist_setup(args)
     device = torch.device("cuda", torch.cuda.current_device())
     from rascil_gb300 import _lib
@@ -498,7 +503,8 @@ def main():
             "gpu_launches": int(launches / args.steps),
             "accuracy_fp32": acc32,
             "plan": {k: info[k] for k in ("support", "sigma", "ngrid_x", "nplanes",
-                                          "planes_per_batch", "tile", "slab", "beta", "dw")},
+                                          "planes_per_batch", "tile", "slab", "beta", "dw",
+                                          "fft_mode")},
             "tuning": tuned,
             "kernels": kernels}
     torch.cuda.empty_cache()

@@ -51,6 +51,15 @@ typedef enum {
 
 typedef enum { GB_FP32 = 0, GB_FP64 = 1 } gb_precision;
 
+/* How the per-plane 2-D transforms run.  GB_FFT_AUTO picks
+ * GB_FFT_COLUMNS where it applies (FP32 form, grid height a power of two
+ * from 256 to 32768), else GB_FFT_CUFFT_2D.  GB_FFT_COLUMNS: batched 1-D
+ * cuFFT rows plus the library's own column kernels, pruned to the image's
+ * columns and fused with the w-screen (asking for it where it does not
+ * apply is GB_ERR_INVALID_ARG).  GB_FFT_CUFFT_2D: batched 2-D cuFFT plans
+ * plus separate screen passes. */
+typedef enum { GB_FFT_AUTO = 0, GB_FFT_CUFFT_2D = 1, GB_FFT_COLUMNS = 2 } gb_fft_mode;
+
 /* Image memory layout.  GB_LAYOUT_XY is ducc0's dirty[x][y] (what
  * ms2dirty returns and dirty2ms takes).  GB_LAYOUT_YX is RASCIL's
  * pixels[..., y, x] (ng.py passes model.T to ducc0, ng.py:94,249), so the
@@ -77,6 +86,7 @@ typedef struct {
   int32_t tile;        /* uv tile side in cells; 0 = default                   */
   int32_t slab;        /* w-planes per bucket slab; 0 = default                */
   int64_t grid_budget_bytes; /* memory for one batch of w-planes; 0 = default  */
+  int32_t fft_mode;    /* gb_fft_mode                                          */
 } gb_plan_params;
 
 /* Geometry the planner chose; all host values. */
@@ -84,6 +94,7 @@ typedef struct {
   int32_t support, ngrid_x, ngrid_y, nplanes, planes_per_batch, tile, slab;
   double beta, sigma, dw, w_lo, w_hi, tc;
   int64_t nitems, nbuckets, workspace_bytes;
+  int32_t fft_mode;    /* the gb_fft_mode in use (never GB_FFT_AUTO)           */
 } gb_plan_info;
 
 typedef struct gb_plan gb_plan;

@@ -54,6 +54,7 @@ class PlanParams(_c.Structure):
         ("tile", _c.c_int32),
         ("slab", _c.c_int32),
         ("grid_budget_bytes", _c.c_int64),
+        ("fft_mode", _c.c_int32),
     ]
 
 
@@ -75,6 +76,7 @@ class PlanInfo(_c.Structure):
         ("nitems", _c.c_int64),
         ("nbuckets", _c.c_int64),
         ("workspace_bytes", _c.c_int64),
+        ("fft_mode", _c.c_int32),
     ]
 
     def as_dict(self):

@@ -1,0 +1,41 @@
+// Column transforms of the FP32 form (gb_fft.cu) and the row order they
+// leave in predict grids.
+#pragma once
+
+#include "gb_plan.cuh"
+
+namespace gb {
+
+struct ColGeom {
+  int n, N1, N2;   // column length n = N1 N2
+  int ox, oy;      // image block offset in the grid
+  int nx, ny;      // image size
+  int64_t plane;   // ngx * ngy
+  int ngx;
+};
+
+// Row order of a predict grid after the column transforms: logical row
+// q = k1 + N1 k2 sits at physical row N2 k1 + k2 = ((q & (N1-1)) << s2) |
+// (q >> s1).  s1 < 0: natural order.
+struct RowPerm {
+  int s1, s2;
+  __host__ __device__ __forceinline__ int row(int q) const {
+    return s1 < 0 ? q : (((q & ((1 << s1) - 1)) << s2) | (q >> s1));
+  }
+};
+
+// True when a column of length n has a supported split n = N1 N2
+// (power of two, 256 <= n <= 32768).
+bool column_split(int n, int &N1, int &N2);
+ColGeom col_geom(const Geom &g);
+RowPerm row_perm(const gb_plan *p);
+
+// Invert: step A in place, then step B fused with the w-screen and the
+// image accumulation (first != 0 starts acc from zero).
+int run_cols_invert(gb_plan *p, void *grid, int b0, int nb, float *acc, int first,
+                    cudaStream_t s);
+// Predict: the screened image through both column steps into the grid's
+// central columns (permuted rows), and zeros in the other columns.
+int run_cols_predict(gb_plan *p, const float *img, int b0, int nb, void *grid, cudaStream_t s);
+
+}  // namespace gb

@@ -18,6 +18,7 @@
 //                           requested layout.
 #include <cufft.h>
 
+#include "gb_fft.cuh"
 #include "gb_plan.cuh"
 
 namespace gb {
@@ -453,6 +454,13 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
       rc = run_fft(p, nb, grid, CUFFT_INVERSE, s);
     }
     if (rc) return rc;
+    if constexpr (std::is_same<R, float>::value) {
+      if (p->col_fft) {  // rows done; columns + screen + accumulate
+        rc = run_cols_invert(p, grid, b0, nb, acc, bi == 0, s);
+        if (rc) return rc;
+        continue;
+      }
+    }
     {
       ProfScope ps(kProfScreenAcc, s,
                    (double)sizeof(C) * nb * NP * npix + (bi ? 2.0 : 1.0) * sizeof(R) * NP * npix);

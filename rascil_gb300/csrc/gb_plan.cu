@@ -14,6 +14,7 @@
 #include <mutex>
 
 #include "es_table.h"
+#include "gb_fft.cuh"
 #include "gb_plan.cuh"
 
 namespace gb {
@@ -541,24 +542,53 @@ static int fft_create(cufftHandle *h) {
   return GB_OK;
 }
 
-// 2-D transforms of `planes` planes x NP pols, batched.  (Pruning the
-// transform to the image's central columns through 1-D strided cuFFT
-// plans measured slower on GB300 than this single batched 2-D plan.)
-static int make_fft_2d(gb_plan *p, int planes, cufftHandle *h, size_t *work) {
+// Transforms of `planes` planes x NP pols, batched: 2-D plans, or in column
+// mode 1-D transforms of every row (the column kernels do the rest).
+// (Pruning to the image's columns through 1-D strided cuFFT plans measured
+// slower on GB300 than the batched 2-D plan; the column kernels replace
+// those strided plans.)
+static int make_fft(gb_plan *p, int planes, cufftHandle *h, size_t *work) {
   const Geom &g = p->g;
   int rc = fft_create(h);
   if (rc) return rc;
-  long long n[2] = {g.ngy, g.ngx};
-  const long long batch = (long long)planes * g.NP;
   const cufftType type = p->precision == GB_FP64 ? CUFFT_Z2Z : CUFFT_C2C;
-  const cufftResult r =
-      cufftMakePlanMany64(*h, 2, n, nullptr, 1, 0, nullptr, 1, 0, type, batch, work);
+  cufftResult r;
+  long long n[2] = {g.ngy, g.ngx};
+  long long batch = (long long)planes * g.NP;
+  if (p->col_fft) {
+    long long nr[1] = {g.ngx};
+    batch *= g.ngy;
+    r = cufftMakePlanMany64(*h, 1, nr, nullptr, 1, 0, nullptr, 1, 0, type, batch, work);
+  } else {
+    r = cufftMakePlanMany64(*h, 2, n, nullptr, 1, 0, nullptr, 1, 0, type, batch, work);
+  }
   if (r != CUFFT_SUCCESS) {
-    set_error("cufftMakePlanMany64 failed (%d) for %lld x %lld x %lld", (int)r, n[0], n[1],
-              batch);
+    set_error("cufftMakePlanMany64 failed (%d) for %lld x %lld x %lld (%s)", (int)r, n[0],
+              n[1], batch, p->col_fft ? "rows" : "2-D");
     return GB_ERR_CUFFT;
   }
   return GB_OK;
+}
+
+// Column mode applies to the FP32 form with a power-of-two grid height.
+static int choose_fft_mode(gb_plan *p) {
+  int n1, n2;
+  const bool fits = p->precision == GB_FP32 && column_split(p->g.ngy, n1, n2);
+  switch (p->params.fft_mode) {
+    case GB_FFT_AUTO: p->col_fft = fits; return GB_OK;
+    case GB_FFT_CUFFT_2D: p->col_fft = false; return GB_OK;
+    case GB_FFT_COLUMNS:
+      if (!fits) {
+        set_error("fft_mode GB_FFT_COLUMNS needs the FP32 form and a power-of-two grid height "
+                  "in [256, 32768] (grid %d x %d)", p->g.ngx, p->g.ngy);
+        return GB_ERR_INVALID_ARG;
+      }
+      p->col_fft = true;
+      return GB_OK;
+    default:
+      set_error("unknown fft_mode %d", p->params.fft_mode);
+      return GB_ERR_INVALID_ARG;
+  }
 }
 
 static int layout_workspace(gb_plan *p) {
@@ -749,6 +779,8 @@ int gb_plan_geometry(const gb_plan_params *params, double w_lo, double w_hi,
   tmp.params = *params;
   tmp.precision = params->precision;
   tmp.fft_work_bytes = 0;
+  rc = choose_fft_mode(&tmp);
+  if (rc) return rc;
   layout_workspace(&tmp);
   memset(info, 0, sizeof(*info));
   info->support = g.W;
@@ -767,6 +799,7 @@ int gb_plan_geometry(const gb_plan_params *params, double w_lo, double w_hi,
   info->nitems = g.nitems;
   info->nbuckets = g.nbuckets;
   info->workspace_bytes = (int64_t)tmp.ws_bytes;
+  info->fft_mode = tmp.col_fft ? GB_FFT_COLUMNS : GB_FFT_CUFFT_2D;
   return GB_OK;
 }
 
@@ -841,7 +874,12 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
   cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, dev);
   // cuFFT plans (host-side; the work area comes from the workspace)
   size_t w_full = 0, w_rem = 0;
-  rc = make_fft_2d(p, p->g.B, &p->fft_full, &w_full);
+  rc = choose_fft_mode(p);
+  if (rc) {
+    gb_plan_destroy(p);
+    return rc;
+  }
+  rc = make_fft(p, p->g.B, &p->fft_full, &w_full);
   if (rc) {
     gb_plan_destroy(p);
     return rc;
@@ -849,7 +887,7 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
   p->fft_full_ok = true;
   p->rem_planes = p->g.nplanes % p->g.B;
   if (p->rem_planes) {
-    rc = make_fft_2d(p, p->rem_planes, &p->fft_rem, &w_rem);
+    rc = make_fft(p, p->rem_planes, &p->fft_rem, &w_rem);
     if (rc) {
       gb_plan_destroy(p);
       return rc;
@@ -938,6 +976,7 @@ int gb_plan_info_get(const gb_plan *p, gb_plan_info *info) {
   info->nitems = g.nitems;
   info->nbuckets = g.nbuckets;
   info->workspace_bytes = (int64_t)p->ws_bytes;
+  info->fft_mode = p->col_fft ? GB_FFT_COLUMNS : GB_FFT_CUFFT_2D;
   return GB_OK;
 }
 

@@ -5,6 +5,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -35,6 +36,9 @@ struct gb_plan {
   cufftHandle fft_full = 0, fft_rem = 0;
   bool fft_full_ok = false, fft_rem_ok = false;
   size_t fft_work_bytes = 0;
+  // column mode (FP32): the plans above are 1-D row transforms and the
+  // column transforms are the library's own kernels (gb_fft.cu)
+  bool col_fft = false;
   size_t off_tprime = 0;  // [ny][nx] float64: n - 1 - tc per pixel (w-stacking)
   bool bound = false;
   bool owns_ws = false;

@@ -19,6 +19,7 @@
 //                           item) or accumulates (later batches) in place.
 #include <cufft.h>
 
+#include "gb_fft.cuh"
 #include "gb_plan.cuh"
 
 namespace gb {
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(kThreads)
              const Chunk *__restrict__ chunks, const uint32_t *__restrict__ chunk_off, int b0,
              int nb, const typename Traits<R>::C *__restrict__ grid,
              typename Traits<R>::C *__restrict__ vis, int npv, const R *__restrict__ wgt,
-             const PolMat pm, uint32_t *__restrict__ counter) {
+             const PolMat pm, const RowPerm rp, uint32_t *__restrict__ counter) {
   using C = typename Traits<R>::C;
   using LM = LaneMap<NP, AW>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -170,9 +171,10 @@ __global__ void __launch_bounds__(kThreads)
           while (q >= g.ngy) q -= g.ngy;
           const R sgn = ((p + q) & 1) ? (R)-1 : (R)1;
           const int cell = y * L.pitch + x;
+          const int64_t row = (int64_t)rp.row(q) * g.ngx;
 #pragma unroll
           for (int pol = 0; pol < NP; ++pol) {
-            const C v = gplane[pol * plane + (int64_t)q * g.ngx + p];
+            const C v = gplane[pol * plane + row + p];
             sg[pol * L.plane + cell] = sgn * v.x;
             sg[(NP + pol) * L.plane + cell] = sgn * v.y;
           }
@@ -211,7 +213,7 @@ __global__ void __launch_bounds__(kThreads)
               const R f = ((p + q) & 1) ? -kv : kv;
 #pragma unroll
               for (int qq = 0; qq < LM::NPL; ++qq) {
-                const C v = gplane[lm.pol(qq) * plane + (int64_t)q * g.ngx + p];
+                const C v = gplane[lm.pol(qq) * plane + (int64_t)rp.row(q) * g.ngx + p];
                 sr[qq] += f * v.x;
                 si[qq] += f * v.y;
               }
@@ -335,11 +337,20 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
   const unsigned cell_blocks = (unsigned)std::min<int64_t>((plane + kThreads - 1) / kThreads,
                                                            (int64_t)p->num_sms * 32);
   const size_t smem = tile_smem_bytes(p);
+  const RowPerm rperm = row_perm(p);
   for (int bi = 0; bi < p->nbatches; ++bi) {
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
     const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
-    {
+    bool cols = false;
+    if constexpr (std::is_same<R, float>::value) {
+      if (p->col_fft) {  // screen + columns now, rows below
+        const int rc = run_cols_predict(p, img, b0, nb, grid, s);
+        if (rc) return rc;
+        cols = true;
+      }
+    }
+    if (!cols) {
       ProfScope ps(kProfScreenPad, s, gbytes + sizeof(R) * NP * npix);
       k_screen_pad<R, NP><<<cell_blocks, kThreads, 0, s>>>(g, img, p->at<double>(p->off_tprime),
                                                            b0, nb, grid);
@@ -358,11 +369,11 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
       if (group_lanes(g.W) == 8)
         k_degrid<R, NP, 8><<<p->degrid_blocks, kThreads, smem, s>>>(
             g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
-            reinterpret_cast<const R *>(wgt), pm, counters + bi);
+            reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
       else
         k_degrid<R, NP, 16><<<p->degrid_blocks, kThreads, smem, s>>>(
             g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
-            reinterpret_cast<const R *>(wgt), pm, counters + bi);
+            reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
       GB_LAUNCH_CHECK("k_degrid");
     }
   }

@@ -59,7 +59,8 @@ const char *kProfNames[kProfCount] = {
     "k_wrange", "k_count", "scan", "k_scatter", "k_chunks", "k_corr_image",
     "k_prep_vis", "k_grid", "cufft_inverse", "k_screen_acc", "k_finalize",
     "k_prep_image", "k_screen_pad", "cufft_forward", "k_degrid", "k_dft_components",
-    "k_dft_pixels"};
+    "k_dft_pixels", "k_col_a_inv", "k_col_b_inv", "k_col_a_pred", "k_col_b_pred",
+    "zero_margins"};
 
 bool prof_on() {
   std::lock_guard<std::mutex> lk(g_mu);

@@ -23,6 +23,11 @@ enum ProfId {
   kProfDegrid,
   kProfDftComp,
   kProfDftPix,
+  kProfColInvA,
+  kProfColInvB,
+  kProfColPredA,
+  kProfColPredB,
+  kProfZeroMargins,
   kProfCount
 };
 

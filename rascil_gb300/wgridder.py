@@ -21,6 +21,8 @@ from . import _lib, tuning
 
 _PREC = {"fp32": _lib.GB_FP32, "fp64": _lib.GB_FP64}
 _LAYOUT = {"xy": _lib.GB_LAYOUT_XY, "yx": _lib.GB_LAYOUT_YX}
+_FFT_MODE = {"auto": 0, "cufft2d": 1, "columns": 2}
+FFT_MODE_NAMES = {1: "cufft2d", 2: "columns"}
 
 
 def _require_cuda(t, name):
@@ -55,11 +57,15 @@ class Plan:
     :param precision: "fp32" (complex64 data) or "fp64" (complex128 data)
     :param bind: allocate a workspace (torch) and run the bucket sort now; with
         ``bind=False`` call :meth:`bind` with a caller-owned buffer later
+    :param fft_mode: "auto" (the library's column kernels where they apply:
+        FP32 form, power-of-two grid height), "columns" (require them) or
+        "cufft2d" (batched 2-D cuFFT plans); ``info["fft_mode"]`` reports
+        the one in use (2 = columns, 1 = cufft2d)
     """
 
     def __init__(self, uvw, freq, npix_x, npix_y, pixsize_x, pixsize_y, epsilon,
                  do_wstacking, npol=1, precision="fp32", sigma=0.0, support=0, tile=0,
-                 slab=0, grid_budget_bytes=0, bind=True):
+                 slab=0, grid_budget_bytes=0, bind=True, fft_mode="auto"):
         lib = _lib.load()
         _require_cuda(uvw, "uvw")
         _require_cuda(freq, "freq")
@@ -69,6 +75,8 @@ class Plan:
             raise ValueError("uvw must be [nrows, 3]")
         if precision not in _PREC:
             raise ValueError("precision must be 'fp32' or 'fp64'")
+        if fft_mode not in _FFT_MODE:
+            raise ValueError("fft_mode must be one of %s" % sorted(_FFT_MODE))
         self.device = uvw.device
         self.precision = precision
         self.npol = int(npol)
@@ -96,6 +104,7 @@ class Plan:
         p.tile = int(tile)
         p.slab = int(slab)
         p.grid_budget_bytes = int(grid_budget_bytes)
+        p.fft_mode = _FFT_MODE[fft_mode]
         self._params = p
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
