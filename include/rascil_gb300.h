@@ -132,6 +132,13 @@ int gb_plan_export_items(const gb_plan *plan, uint32_t *bucket_dev, int32_t *cel
 /* Release host resources (cuFFT plans).  Never frees the workspace. */
 int gb_plan_destroy(gb_plan *plan);
 
+/* Device status of a bound plan: waits for `stream`, returns in *status_out
+ * the error bits kernels recorded since the last call (0 = none; 1 = a
+ * TMA completion wait ran past its iteration limit, so that call's output
+ * is invalid) and clears them.  No counterpart in the reference (its CPU
+ * gridder has no device waits). */
+int gb_plan_device_status(gb_plan *plan, void *stream, int32_t *status_out);
+
 /* Invert: dirty image from visibilities.  Replaces ducc0 ms2dirty
  * (ng.py:232-248 MFS, 259-275 per channel) for all npol polarisations
  * in one pass.

@@ -91,6 +91,7 @@ SIGNATURES = {
     "gb_plan_bind": (_c.c_int, [_vp, _vp, _c.c_size_t, _vp]),
     "gb_plan_info_get": (_c.c_int, [_vp, _c.POINTER(PlanInfo)]),
     "gb_plan_destroy": (_c.c_int, [_vp]),
+    "gb_plan_device_status": (_c.c_int, [_vp, _vp, _c.POINTER(_c.c_int32)]),
     "gb_plan_export_items": (_c.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "gb_plan_ms2dirty": (_c.c_int, [_vp, _vp, _c.c_int32, _vp, _vp, _c.c_int32, _dp,
                                     _c.c_int32, _vp, _c.c_int32, _vp, _vp]),

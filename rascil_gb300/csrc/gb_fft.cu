@@ -1,42 +1,69 @@
-// Fused, pruned column transforms for power-of-two grid heights (FP32 form).
+// Fused, pruned column transforms of the FP32 form.
 //
 // A w-plane's 2-D transform is done as row transforms (batched 1-D cuFFT
-// over contiguous rows) plus column transforms written here.  The image
-// occupies only the nx central columns and ny central rows of each plane
-// (checkerboarded grids), so only those columns are transformed, by a
-// four-step split of the column length n = N1 N2 (q = N2 q1 + q2,
-// k = k1 + N1 k2):
+// over contiguous rows) plus column transforms written here.  Column mode
+// applies when the grid height is a power of two and exactly twice the
+// image height (sigma = 2), so the image occupies the middle half of every
+// column (checkerboarded grids) and only the image's nx columns need
+// transforms.  The column length n = N1 N2 is split four-step
+// (q = N2 q1 + q2, k = k1 + N1 k2):
 //
 //   step A  for each q2: the N1-point DFT over q1 of x[N2 q1 + q2], times
 //           exp(s 2 pi i q2 k1 / n), stored back at rows N2 k1 + q2;
 //   step B  for each k1: the N2-point DFT over the contiguous rows
 //           N2 k1 + q2 gives X[k1 + N1 k2].
 //
-// A CTA transforms a tile of kTC = 16 adjacent columns (128-byte row
-// segments) with radix-8/4/2 Stockham passes in shared memory.  Fusions:
+// Each CTA transforms a tile of kCW = 32 adjacent columns (256-byte row
+// segments; lane = column).  A column of length N is split N = T M over
+// the T warps: warp t holds elements t + T m (m < M) in registers, does an
+// M-point DFT in registers, multiplies by exp(s 2 pi i t k1 / N), and one
+// exchange through shared memory gives each warp the T-point DFTs of
+// outputs k1 + M k2 -- one shared-memory round trip per tile instead of a
+// pass per radix stage.
 //
+// Fusions:
 //   invert  (rows first, then columns)  step B never writes the plane back:
-//           it keeps only the image rows, applies each plane's w-screen
-//           exp(-2 pi i w_k (n-1-tc)) and accumulates the image in registers
-//           over the batch's planes, so a batch costs one read-modify-write
-//           of the image instead of a pass over every plane;
+//           it keeps only the image rows (outputs k2 in [T/4, 3T/4) of every
+//           warp), applies each plane's w-screen and accumulates the image
+//           in registers over the batch's planes and pols, with the next
+//           tile's loads in flight (cp.async, double-buffered);
 //   predict (columns first, then rows)  step A builds its input from the
-//           corrected image (screen exp(+2 pi i w_k (n-1-tc)) on the image
-//           rows, zero elsewhere) instead of reading a padded grid, and
-//           step B writes in place, so physical row N2 k1 + k2 holds logical
-//           row k1 + N1 k2; the degridder reads rows through that
-//           permutation (RowPerm).
+//           corrected image (inputs m in [M/4, 3M/4) of every warp, zero
+//           elsewhere) times each plane's w-screen, and step B writes in
+//           place, so physical row N2 k1 + k2 holds logical row k1 + N1 k2;
+//           the degridder reads rows through that permutation (RowPerm).
+//
+// The w-screen of plane k at a pixel is exp(s 2 pi i (A + k D)) with A, D the
+// pixel's FP64 phase terms stored as 64-bit fixed-point turns, so the
+// per-plane phase is exact integer arithmetic (no FP64 work per plane) and
+// only the final sincos of the reduced phase is FP32.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cufft.h>
+
+#include <mutex>
 
 #include "gb_fft.cuh"
 
 namespace gb {
 
-constexpr int kTC = 16;  // columns per tile
+constexpr int kCW = 32;  // columns per tile: one lane per column
+
+template <int N>
+struct ColShape {
+  static constexpr int T = N <= 32 ? 4 : (N <= 128 ? 8 : 16);  // warps per column tile
+  static constexpr int M = N / T;                              // elements per thread
+  static constexpr int THREADS = kCW * T;
+  static_assert(M % T == 0 && M % 4 == 0 && T % 4 == 0, "column split");
+};
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 cmulc(float2 a, float c, float s) {
+  return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 // a * (s i)
@@ -44,13 +71,7 @@ template <int S> __device__ __forceinline__ float2 mul_si(float2 a) {
   return S > 0 ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// In-register R-point DFTs, z_q = sum_p a_p exp(s 2 pi i p q / R).
-template <int S> __device__ __forceinline__ void dft2(float2 *a) {
-  const float2 t = a[0];
-  a[0] = cadd(t, a[1]);
-  a[1] = csub(t, a[1]);
-}
-
+// In-register L-point DFTs in natural order, z_q = sum_p a_p exp(s 2 pi i p q / L).
 template <int S> __device__ __forceinline__ void dft4(float2 *a) {
   const float2 s02 = cadd(a[0], a[2]), d02 = csub(a[0], a[2]);
   const float2 s13 = cadd(a[1], a[3]), d13 = mul_si<S>(csub(a[1], a[3]));
@@ -60,14 +81,17 @@ template <int S> __device__ __forceinline__ void dft4(float2 *a) {
   a[3] = csub(d02, d13);
 }
 
+constexpr float kR2 = 0.70710678118654752f;  // cos(pi/4)
+constexpr float kC8 = 0.92387953251128674f;  // cos(pi/8)
+constexpr float kS8 = 0.38268343236508977f;  // sin(pi/8)
+
 template <int S> __device__ __forceinline__ void dft8(float2 *a) {
   float2 e[4] = {a[0], a[2], a[4], a[6]};
   float2 o[4] = {a[1], a[3], a[5], a[7]};
   dft4<S>(e);
   dft4<S>(o);
-  const float r = 0.70710678118654752f;  // cos(pi/4)
-  const float2 w1 = make_float2(r, S * r), w3 = make_float2(-r, S * r);
-  const float2 t0 = o[0], t1 = cmul(o[1], w1), t2 = mul_si<S>(o[2]), t3 = cmul(o[3], w3);
+  const float2 t0 = o[0], t1 = cmulc(o[1], kR2, S * kR2), t2 = mul_si<S>(o[2]),
+               t3 = cmulc(o[3], -kR2, S * kR2);
   a[0] = cadd(e[0], t0);
   a[4] = csub(e[0], t0);
   a[1] = cadd(e[1], t1);
@@ -78,258 +102,372 @@ template <int S> __device__ __forceinline__ void dft8(float2 *a) {
   a[7] = csub(e[3], t3);
 }
 
-template <int R, int S> __device__ __forceinline__ void dftR(float2 *a) {
-  if (R == 2) dft2<S>(a);
-  else if (R == 4) dft4<S>(a);
-  else dft8<S>(a);
+// 16 = 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2.
+template <int S> __device__ __forceinline__ void dft16(float2 *a) {
+  float2 y[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    float2 b[4] = {a[n2], a[4 + n2], a[8 + n2], a[12 + n2]};
+    dft4<S>(b);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = b[k1];
+  }
+  // twiddles exp(s 2 pi i n2 k1 / 16)
+  y[1][1] = cmulc(y[1][1], kC8, S * kS8);
+  y[1][2] = cmulc(y[1][2], kR2, S * kR2);
+  y[1][3] = cmulc(y[1][3], kS8, S * kC8);
+  y[2][1] = cmulc(y[2][1], kR2, S * kR2);
+  y[2][2] = mul_si<S>(y[2][2]);
+  y[2][3] = cmulc(y[2][3], -kR2, S * kR2);
+  y[3][1] = cmulc(y[3][1], kS8, S * kC8);
+  y[3][2] = cmulc(y[3][2], -kR2, S * kR2);
+  y[3][3] = cmulc(y[3][3], -kC8, -S * kS8);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 b[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    dft4<S>(b);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) a[k1 + 4 * k2] = b[k2];
+  }
 }
 
-// One Stockham pass of radix R over the [L][kTC] tile in `x`, in place:
-// every thread loads the inputs of its butterflies into registers, the
-// block synchronises, and the outputs overwrite the same buffer.
-// tw[m] = exp(s 2 pi i m / L).
-template <int L, int R, int S>
-__device__ __forceinline__ void stockham_pass(float2 *x, int Ls, const float2 *__restrict__ tw) {
-  constexpr int NB = L / R;
-  constexpr int NBF = NB * kTC;  // butterflies in the tile
-  constexpr int BPT = (NBF + kThreads - 1) / kThreads;
-  const int tstep = L / (Ls * R);
-  float2 a[BPT][R];
+template <int L, int S> __device__ __forceinline__ void dft(float2 *a) {
+  if constexpr (L == 4) dft4<S>(a);
+  else if constexpr (L == 8) dft8<S>(a);
+  else dft16<S>(a);
+}
+
+// N-point DFT of every column of a tile.  On entry x[m] holds column
+// element t + T m of this thread's column (lane c, warp t); on exit
+// y[ii][k2] holds output k1 + M k2 with k1 = t + T ii.  xb: N * kCW
+// exchange slots; this thread writes only slots (r T + t) kCW + c, r < M,
+// before the barrier.  The caller synchronises before xb is reused.
+// tw[m] = exp(s 2 pi i m / N).
+template <int N, int S>
+__device__ __forceinline__ void col_dft(float2 (&x)[ColShape<N>::M], float2 *__restrict__ xb,
+                                        const float2 *__restrict__ tw, int t, int c,
+                                        float2 (&y)[ColShape<N>::M / ColShape<N>::T]
+                                                   [ColShape<N>::T]) {
+  constexpr int T = ColShape<N>::T, M = ColShape<N>::M;
+  dft<M, S>(x);
 #pragma unroll
-  for (int t = 0; t < BPT; ++t) {
-    const int b = threadIdx.x + t * kThreads;
-    if (NBF % kThreads == 0 || b < NBF) {
-      const int c = b % kTC, j = b / kTC;
-      const int k = j & (Ls - 1);
+  for (int k1 = 1; k1 < M; ++k1) x[k1] = cmul(x[k1], tw[t * k1]);
 #pragma unroll
-      for (int p = 0; p < R; ++p) {
-        a[t][p] = x[(j + p * NB) * kTC + c];
-        if (p > 0) a[t][p] = cmul(a[t][p], tw[(p * k * tstep) & (L - 1)]);
-      }
-      dftR<R, S>(a[t]);
-    }
-  }
+  for (int k1 = 0; k1 < M; ++k1) xb[(k1 * T + t) * kCW + c] = x[k1];
   __syncthreads();
 #pragma unroll
-  for (int t = 0; t < BPT; ++t) {
-    const int b = threadIdx.x + t * kThreads;
-    if (NBF % kThreads == 0 || b < NBF) {
-      const int c = b % kTC, j = b / kTC;
-      const int k = j & (Ls - 1);
-      const int base = (j - k) * R + k;
+  for (int ii = 0; ii < M / T; ++ii) {
+    const int k1 = t + T * ii;
 #pragma unroll
-      for (int q = 0; q < R; ++q) x[(base + q * Ls) * kTC + c] = a[t][q];
-    }
-  }
-  __syncthreads();
-}
-
-// Natural-order L-point transform of every column of the tile, in place.
-// Radix plan: as many radix-8 passes as fit, then one radix-4 or radix-2.
-// The caller synchronises before (tile and twiddles written).
-template <int L, int S>
-__device__ __forceinline__ void tile_fft(float2 *x, const float2 *tw) {
-  constexpr int lg = L == 256 ? 8 : L == 128 ? 7 : L == 64 ? 6 : L == 32 ? 5 : 4;
-  static_assert((1 << lg) == L, "tile length must be 16..256");
-  constexpr int e8 = lg / 3, rem = lg % 3;
-  int Ls = 1;
-#pragma unroll
-  for (int i = 0; i < e8; ++i) {
-    stockham_pass<L, 8, S>(x, Ls, tw);
-    Ls *= 8;
-  }
-  if (rem == 2) stockham_pass<L, 4, S>(x, Ls, tw);
-  if (rem == 1) stockham_pass<L, 2, S>(x, Ls, tw);
-}
-
-template <int L, int S>
-__device__ __forceinline__ void make_twiddles(float2 *tw) {
-  for (int m = threadIdx.x; m < L; m += blockDim.x) {
-    float s, c;
-    sincospif(2.0f * (float)m / (float)L, &s, &c);
-    tw[m] = make_float2(c, S * s);
+    for (int tt = 0; tt < T; ++tt) y[ii][tt] = xb[(k1 * T + tt) * kCW + c];
+    dft<T, S>(y[ii]);
   }
 }
 
-// exp(s 2 pi i q2 k1 / n) for k1 in [0, N1): exact integer angle.
-template <int N1, int S>
-__device__ __forceinline__ void make_step_twiddles(float2 *st, int q2, int n) {
-  for (int k1 = threadIdx.x; k1 < N1; k1 += blockDim.x) {
-    const int m = (q2 * k1) & (n - 1);
-    float s, c;
-    sincospif(2.0f * (float)m / (float)n, &s, &c);
-    st[k1] = make_float2(c, S * s);
+// exp(s 2 pi i m / N), m < N, from the n-point table exp(+2 pi i m / n).
+template <int N, int S>
+__device__ __forceinline__ void load_twiddles(float2 *tw, const float2 *__restrict__ twn, int n) {
+  const int step = n / N;
+  for (int m = threadIdx.x; m < N; m += blockDim.x) {
+    const float2 w = twn[m * step];
+    tw[m] = S > 0 ? w : conjf2(w);
   }
+}
+
+// sin / cos of plane k's w-screen phase 2 pi (A + k D) at a pixel.
+__device__ __forceinline__ void screen_sincos(ulonglong2 ad, int k, float *sn, float *cs) {
+  const unsigned long long ph = ad.x + (unsigned long long)(unsigned)k * ad.y;
+  const int hi = (int)(unsigned)(ph >> 32);  // turns * 2^32 in [-2^31, 2^31)
+  sincospif((float)hi * 0x1p-31f, sn, cs);
+}
+
+__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gmem_src, bool valid) {
+  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(gmem_src),
+               "r"(valid ? 8 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// TMA (bulk tensor copies) with mbarrier completion.
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbarrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
+      "{%2, %3}], [%4];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait for the phase with the given parity to complete.
+constexpr int kMbarSpins = 1 << 20;
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+  for (int i = 0; i < kMbarSpins; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
 }
 
 // ----------------------------------------------------------------------
-// invert step A: in place on the grid, one CTA per (column tile, q2, plane-pol).
+// invert step A: in place, one CTA per (column tile, q2, plane-pol).
 template <int N1>
-__global__ void __launch_bounds__(kThreads) k_col_a_inv(const ColGeom cg, float2 *__restrict__ grid) {
-  __shared__ float2 buf[N1 * kTC];
-  __shared__ float2 tw[N1], st[N1];
-  const int p0 = cg.ox + blockIdx.x * kTC;
+__global__ void __launch_bounds__(ColShape<N1>::THREADS, 3)
+    k_cols_a_inv(const ColGeom cg, const float2 *__restrict__ twn, float2 *__restrict__ grid) {
+  using CS = ColShape<N1>;
+  constexpr int T = CS::T, M = CS::M;
+  extern __shared__ float2 smem[];
+  float2 *xb = smem, *tw = smem + N1 * kCW;
+  const int c = threadIdx.x % kCW, t = threadIdx.x / kCW;
+  const int p = cg.ox + blockIdx.x * kCW + c;
+  const bool ok = p < cg.ox + cg.nx;
   const int q2 = blockIdx.y;
   float2 *plane = grid + (int64_t)blockIdx.z * cg.plane;
-  make_twiddles<N1, 1>(tw);
-  make_step_twiddles<N1, 1>(st, q2, cg.n);
-  const int pend = cg.ox + cg.nx;
-  for (int e = threadIdx.x; e < N1 * kTC; e += kThreads) {
-    const int c = e % kTC, q1 = e / kTC;
-    const int p = p0 + c;
-    buf[e] = p < pend ? plane[(int64_t)(cg.N2 * q1 + q2) * cg.ngx + p] : make_float2(0.f, 0.f);
-  }
+  load_twiddles<N1, 1>(tw, twn, cg.n);
+  float2 x[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+    x[m] = ok ? plane[(int64_t)(cg.N2 * (t + T * m) + q2) * cg.ngx + p] : make_float2(0.f, 0.f);
   __syncthreads();
-  tile_fft<N1, 1>(buf, tw);
-  for (int e = threadIdx.x; e < N1 * kTC; e += kThreads) {
-    const int c = e % kTC, k1 = e / kTC;
-    const int p = p0 + c;
-    if (p < pend) plane[(int64_t)(cg.N2 * k1 + q2) * cg.ngx + p] = cmul(buf[e], st[k1]);
+  float2 y[M / T][T];
+  col_dft<N1, 1>(x, xb, tw, t, c, y);
+  if (ok) {
+#pragma unroll
+    for (int ii = 0; ii < M / T; ++ii)
+#pragma unroll
+      for (int k2 = 0; k2 < T; ++k2) {
+        const int o = t + T * ii + M * k2;
+        plane[(int64_t)(cg.N2 * o + q2) * cg.ngx + p] = cmul(y[ii][k2], twn[q2 * o]);
+      }
   }
 }
 
-// invert step B + w-screen + accumulate: one CTA per (column tile, k1); it
-// loops over the batch's planes (and pols), accumulating the image pixels it
-// owns in registers, and updates acc once.
+// invert step B + w-screen + accumulate: one CTA per (column tile, k1).
+// The batch's nb x NP plane-pols stream through two shared-memory tile
+// buffers filled by TMA (one 2-D box of N2 rows x 32 columns per tile,
+// completion on an mbarrier), so the next tile is in flight while this one
+// is transformed; the kept outputs accumulate in per-thread shared-memory
+// slots.  A wait that runs past its iteration limit records kErrTmaTimeout
+// in *status, drains the other buffer (bounded) and returns.
 template <int N2, int NP>
-__global__ void __launch_bounds__(kThreads)
-    k_col_b_inv(const ColGeom cg, const Geom g, const float2 *__restrict__ grid, int b0, int nb,
-                const double *__restrict__ tprime, float *__restrict__ acc, int first) {
-  constexpr int EPT = (N2 * kTC + kThreads - 1) / kThreads;
-  __shared__ float2 buf[N2 * kTC];
-  __shared__ float2 tw[N2];
-  const int p0 = cg.ox + blockIdx.x * kTC;
-  const int k1 = blockIdx.y;
-  const int pend = cg.ox + cg.nx;
-  make_twiddles<N2, 1>(tw);
+__global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 2)
+    k_cols_b_inv(const __grid_constant__ CUtensorMap tmap, const ColGeom cg,
+                 const float2 *__restrict__ twn, const ulonglong2 *__restrict__ screen, int do_w,
+                 int b0, int nb, float *__restrict__ acc, int first,
+                 uint32_t *__restrict__ status) {
+  using CS = ColShape<N2>;
+  constexpr int T = CS::T, M = CS::M, MT = M / T, KL = T / 4, KK = T / 2;
+  constexpr int NK = MT * KK;  // kept outputs per thread
+  constexpr unsigned kTileBytes = N2 * kCW * sizeof(float2);
+  // dynamic shared memory only (TMA destinations at 128-byte offsets):
+  // two tiles | twiddles | accumulators | 2 mbarriers | abort flag
+  extern __shared__ __align__(128) float2 smem[];
+  auto buf = [&](int s) { return smem + (s & 1) * (N2 * kCW); };
+  float2 *tw = smem + 2 * N2 * kCW;
+  float *sacc = reinterpret_cast<float *>(tw + N2);  // [NP][NK][T][kCW]
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sacc + NP * NK * T * kCW);
+  int &s_abort = *reinterpret_cast<int *>(bar + 2);
+  const int c = threadIdx.x % kCW, t = threadIdx.x / kCW;
+  const int p0 = cg.ox + blockIdx.x * kCW;
+  const int p = p0 + c;
+  const bool ok = p < cg.ox + cg.nx;
+  const int ix = p - cg.ox;
+  const int k1o = blockIdx.y;
   const int64_t npix = (int64_t)cg.nx * cg.ny;
-  int pix[EPT];  // image pixel of element e, or -1
-  float a[NP][EPT];
-#pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    const int e = threadIdx.x + i * kThreads;
-    pix[i] = -1;
-    if (e < N2 * kTC) {
-      const int c = e % kTC, k2 = e / kTC;
-      const int iy = k1 + cg.N1 * k2 - cg.oy, ix = p0 + c - cg.ox;
-      if (iy >= 0 && iy < cg.ny && ix < cg.nx) pix[i] = iy * cg.nx + ix;
-    }
-#pragma unroll
-    for (int p = 0; p < NP; ++p) a[p][i] = (first || pix[i] < 0) ? 0.f : acc[p * npix + pix[i]];
+  const int iters = nb * NP;
+  // tile s = plane-pol s of the batch buffer: rows s ngy + N2 k1o + [0, N2)
+  auto issue = [&](int s) {
+    fence_proxy_async();  // earlier generic writes to the buffer before the async copy
+    mbar_expect_tx(&bar[s & 1], kTileBytes);
+    tma_load_2d(buf(s), &tmap, p0, s * cg.n + cg.N2 * k1o, &bar[s & 1]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    s_abort = 0;
+    fence_mbarrier_init();
   }
+  load_twiddles<N2, 1>(tw, twn, cg.n);
+  __syncthreads();
+  if (threadIdx.x == 0) issue(0);
+  // kept output e = ii KK + kk: o = t + T ii + M (KL + kk), image row k1o + N1 o - oy
+  auto pixel = [&](int e) {
+    const int ii = e / KK, kk = e - ii * KK;
+    const int o = t + T * ii + M * (KL + kk);
+    return (int64_t)(k1o + cg.N1 * o - cg.oy) * cg.nx + ix;
+  };
+  auto slot = [&](int pol, int e) { return ((pol * NK + e) * T + t) * kCW + c; };
+#pragma unroll 1
+  for (int pol = 0; pol < NP; ++pol)
+#pragma unroll
+    for (int e = 0; e < NK; ++e)
+      sacc[slot(pol, e)] = (first || !ok) ? 0.f : acc[pol * npix + pixel(e)];
+  int s = 0;
   for (int j = 0; j < nb; ++j) {
-    float sn[EPT], cs[EPT];
+    float sn[NK], cs[NK];
 #pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      sn[i] = 0.f;
-      cs[i] = 1.f;
-      if (g.do_w && pix[i] >= 0)
-        sincos_2pi((float)plane_turns(g, b0 + j, tprime[pix[i]]), &sn[i], &cs[i]);
+    for (int e = 0; e < NK; ++e) {
+      sn[e] = 0.f;
+      cs[e] = 1.f;
+      if (do_w && ok) screen_sincos(screen[pixel(e)], b0 + j, &sn[e], &cs[e]);
     }
+#pragma unroll 1
+    for (int pol = 0; pol < NP; ++pol, ++s) {
+      if (threadIdx.x == 0 && s + 1 < iters) issue(s + 1);
+      float2 *cur = buf(s);
+      if (!mbar_wait(&bar[s & 1], (s >> 1) & 1)) s_abort = 1;
+      float2 x[M];
 #pragma unroll
-    for (int pol = 0; pol < NP; ++pol) {
-      const float2 *plane = grid + ((int64_t)j * NP + pol) * cg.plane;
-      for (int e = threadIdx.x; e < N2 * kTC; e += kThreads) {
-        const int c = e % kTC, q2 = e / kTC;
-        const int p = p0 + c;
-        buf[e] = p < pend ? plane[(int64_t)(cg.N2 * k1 + q2) * cg.ngx + p] : make_float2(0.f, 0.f);
+      for (int m = 0; m < M; ++m) x[m] = cur[(m * T + t) * kCW + c];
+      float2 y[MT][T];
+      col_dft<N2, 1>(x, cur, tw, t, c, y);
+#pragma unroll
+      for (int e = 0; e < NK; ++e) {
+        const float2 v = y[e / KK][KL + e % KK];
+        sacc[slot(pol, e)] += v.x * cs[e] + v.y * sn[e];  // Re(v exp(-i theta))
       }
-      __syncthreads();
-      tile_fft<N2, 1>(buf, tw);
-#pragma unroll
-      for (int i = 0; i < EPT; ++i) {
-        const int e = threadIdx.x + i * kThreads;
-        if (pix[i] >= 0) {
-          const float2 v = buf[e];
-          a[pol][i] += v.x * cs[i] + v.y * sn[i];  // Re(v exp(-i theta))
+      __syncthreads();  // tile s consumed before its buffer is refilled
+      if (s_abort) {
+        if (threadIdx.x == 0) {
+          atomicOr(status, kErrTmaTimeout);
+          if (s + 1 < iters) mbar_wait(&bar[(s + 1) & 1], ((s + 1) >> 1) & 1);
         }
+        return;
       }
-      __syncthreads();
     }
   }
+  if (ok) {
+#pragma unroll 1
+    for (int pol = 0; pol < NP; ++pol)
 #pragma unroll
-  for (int i = 0; i < EPT; ++i)
-    if (pix[i] >= 0)
-#pragma unroll
-      for (int p = 0; p < NP; ++p) acc[p * npix + pix[i]] = a[p][i];
+      for (int e = 0; e < NK; ++e) acc[pol * npix + pixel(e)] = sacc[slot(pol, e)];
+  }
 }
 
-// predict step A from the corrected image: one CTA per (column tile, q2, pol),
-// looping over the batch's planes, so the image tile is read once.
+// predict step A from the corrected image: one CTA per (column tile, q2);
+// loops over the batch's planes and the pols.  The image values (inputs
+// m in [M/4, 3M/4) of each thread) and each plane's screens sit in
+// per-thread shared-memory slots.
 template <int N1, int NP>
-__global__ void __launch_bounds__(kThreads)
-    k_col_a_pred(const ColGeom cg, const Geom g, const float *__restrict__ img,
-                 const double *__restrict__ tprime, int b0, int nb, float2 *__restrict__ grid) {
-  constexpr int EPT = (N1 * kTC + kThreads - 1) / kThreads;
-  __shared__ float2 buf[N1 * kTC];
-  __shared__ float2 tw[N1], st[N1];
-  const int p0 = cg.ox + blockIdx.x * kTC;
+__global__ void __launch_bounds__(ColShape<N1>::THREADS, 2)
+    k_cols_a_pred(const ColGeom cg, const float2 *__restrict__ twn, const float *__restrict__ img,
+                  const ulonglong2 *__restrict__ screen, int do_w, int b0, int nb,
+                  float2 *__restrict__ grid) {
+  using CS = ColShape<N1>;
+  constexpr int T = CS::T, M = CS::M, ML = M / 4, MK = M / 2;
+  extern __shared__ float2 smem[];
+  float2 *xb = smem, *tw = smem + N1 * kCW;
+  float2 *st = tw + N1;                                  // exp(-2 pi i q2 o / n), o < N1
+  float2 *scr = st + N1;                                 // [MK][T][kCW] (cos, sin)
+  float *sv = reinterpret_cast<float *>(scr + MK * T * kCW);  // [NP][MK][T][kCW]
+  const int c = threadIdx.x % kCW, t = threadIdx.x / kCW;
+  const int p = cg.ox + blockIdx.x * kCW + c;
+  const bool ok = p < cg.ox + cg.nx;
+  const int ix = p - cg.ox;
   const int q2 = blockIdx.y;
-  const int pol = blockIdx.z;
-  const int pend = cg.ox + cg.nx;
-  make_twiddles<N1, -1>(tw);
-  make_step_twiddles<N1, -1>(st, q2, cg.n);
   const int64_t npix = (int64_t)cg.nx * cg.ny;
-  float v[EPT];
-  int pix[EPT];
+  load_twiddles<N1, -1>(tw, twn, cg.n);
+  for (int o = threadIdx.x; o < N1; o += blockDim.x) st[o] = conjf2(twn[q2 * o]);
+  // image input mm: row N2 (t + T (ML + mm)) + q2 of the grid, minus oy
+  auto pixel = [&](int mm) {
+    const int q = cg.N2 * (t + T * (ML + mm)) + q2;
+    return (int64_t)(q - cg.oy) * cg.nx + ix;
+  };
+  auto slot = [&](int mm) { return (mm * T + t) * kCW + c; };
+#pragma unroll 1
+  for (int pol = 0; pol < NP; ++pol)
 #pragma unroll
-  for (int i = 0; i < EPT; ++i) {
-    const int e = threadIdx.x + i * kThreads;
-    v[i] = 0.f;
-    pix[i] = -1;
-    if (e < N1 * kTC) {
-      const int c = e % kTC, q1 = e / kTC;
-      const int iy = cg.N2 * q1 + q2 - cg.oy, ix = p0 + c - cg.ox;
-      if (iy >= 0 && iy < cg.ny && ix < cg.nx) {
-        pix[i] = iy * cg.nx + ix;
-        v[i] = img[pol * npix + pix[i]];
-      }
-    }
-  }
+    for (int mm = 0; mm < MK; ++mm)
+      sv[pol * MK * T * kCW + slot(mm)] = ok ? img[pol * npix + pixel(mm)] : 0.f;
+  __syncthreads();  // twiddles
   for (int j = 0; j < nb; ++j) {
-    float2 *plane = grid + ((int64_t)j * NP + pol) * cg.plane;
 #pragma unroll
-    for (int i = 0; i < EPT; ++i) {
-      const int e = threadIdx.x + i * kThreads;
-      if (e < N1 * kTC) {
-        float sn = 0.f, cs = 1.f;
-        if (g.do_w && pix[i] >= 0)
-          sincos_2pi((float)plane_turns(g, b0 + j, tprime[pix[i]]), &sn, &cs);
-        buf[e] = make_float2(v[i] * cs, v[i] * sn);
+    for (int mm = 0; mm < MK; ++mm) {
+      float sn = 0.f, cs = 1.f;
+      if (do_w && ok) screen_sincos(screen[pixel(mm)], b0 + j, &sn, &cs);
+      scr[slot(mm)] = make_float2(cs, sn);
+    }
+#pragma unroll 1
+    for (int pol = 0; pol < NP; ++pol) {
+      float2 x[M];
+#pragma unroll
+      for (int m = 0; m < M; ++m) x[m] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int mm = 0; mm < MK; ++mm) {
+        const float2 e = scr[slot(mm)];
+        const float v = sv[pol * MK * T * kCW + slot(mm)];
+        x[ML + mm] = make_float2(v * e.x, v * e.y);
       }
+      float2 y[M / T][T];
+      col_dft<N1, -1>(x, xb, tw, t, c, y);
+      if (ok) {
+        float2 *plane = grid + ((int64_t)j * NP + pol) * cg.plane;
+#pragma unroll
+        for (int ii = 0; ii < M / T; ++ii)
+#pragma unroll
+          for (int k2 = 0; k2 < T; ++k2) {
+            const int o = t + T * ii + M * k2;
+            plane[(int64_t)(cg.N2 * o + q2) * cg.ngx + p] = cmul(y[ii][k2], st[o]);
+          }
+      }
+      __syncthreads();  // exchange slots free again
     }
-    __syncthreads();
-    tile_fft<N1, -1>(buf, tw);
-    for (int e = threadIdx.x; e < N1 * kTC; e += kThreads) {
-      const int c = e % kTC, k1 = e / kTC;
-      const int p = p0 + c;
-      if (p < pend) plane[(int64_t)(cg.N2 * k1 + q2) * cg.ngx + p] = cmul(buf[e], st[k1]);
-    }
-    __syncthreads();
   }
 }
 
 // predict step B: in place, one CTA per (column tile, k1, plane-pol).
 template <int N2>
-__global__ void __launch_bounds__(kThreads) k_col_b_pred(const ColGeom cg, float2 *__restrict__ grid) {
-  __shared__ float2 buf[N2 * kTC];
-  __shared__ float2 tw[N2];
-  const int p0 = cg.ox + blockIdx.x * kTC;
+__global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 3)
+    k_cols_b_pred(const ColGeom cg, const float2 *__restrict__ twn, float2 *__restrict__ grid) {
+  using CS = ColShape<N2>;
+  constexpr int T = CS::T, M = CS::M;
+  extern __shared__ float2 smem[];
+  float2 *xb = smem, *tw = smem + N2 * kCW;
+  const int c = threadIdx.x % kCW, t = threadIdx.x / kCW;
+  const int p = cg.ox + blockIdx.x * kCW + c;
+  const bool ok = p < cg.ox + cg.nx;
   const int k1 = blockIdx.y;
-  const int pend = cg.ox + cg.nx;
   float2 *plane = grid + (int64_t)blockIdx.z * cg.plane;
-  make_twiddles<N2, -1>(tw);
-  for (int e = threadIdx.x; e < N2 * kTC; e += kThreads) {
-    const int c = e % kTC, q2 = e / kTC;
-    const int p = p0 + c;
-    buf[e] = p < pend ? plane[(int64_t)(cg.N2 * k1 + q2) * cg.ngx + p] : make_float2(0.f, 0.f);
-  }
+  load_twiddles<N2, -1>(tw, twn, cg.n);
+  float2 x[M];
+#pragma unroll
+  for (int m = 0; m < M; ++m)
+    x[m] = ok ? plane[(int64_t)(cg.N2 * k1 + t + T * m) * cg.ngx + p] : make_float2(0.f, 0.f);
   __syncthreads();
-  tile_fft<N2, -1>(buf, tw);
-  for (int e = threadIdx.x; e < N2 * kTC; e += kThreads) {
-    const int c = e % kTC, k2 = e / kTC;
-    const int p = p0 + c;
-    if (p < pend) plane[(int64_t)(cg.N2 * k1 + k2) * cg.ngx + p] = buf[e];
+  float2 y[M / T][T];
+  col_dft<N2, -1>(x, xb, tw, t, c, y);
+  if (ok) {
+#pragma unroll
+    for (int ii = 0; ii < M / T; ++ii)
+#pragma unroll
+      for (int k2 = 0; k2 < T; ++k2)
+        plane[(int64_t)(cg.N2 * k1 + t + T * ii + M * k2) * cg.ngx + p] = y[ii][k2];
   }
 }
 
@@ -376,19 +514,103 @@ RowPerm row_perm(const gb_plan *p) {
   return rp;
 }
 
+// exchange slots + twiddles
+template <int N> constexpr size_t smem_one() { return sizeof(float2) * ((size_t)N * kCW + N); }
+// + screen slots and image slots (N/2 inputs per column)
+template <int N, int NP> constexpr size_t smem_a_pred() {
+  return smem_one<N>() + sizeof(float2) * N +
+         (sizeof(float2) + sizeof(float) * NP) * (size_t)(N / 2) * kCW;
+}
+// two tile buffers + twiddles + accumulator slots (N/2 kept outputs per column)
+template <int N, int NP> constexpr size_t smem_b_inv() {
+  return sizeof(float2) * ((size_t)2 * N * kCW + N) + sizeof(float) * NP * (size_t)(N / 2) * kCW +
+         2 * sizeof(uint64_t) + 16;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// link against the driver library).
+static PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+// 2-D map over the batch buffer viewed as rows of ngx 8-byte cells
+// (B NP ngy rows); box = 32 cells x box_rows rows.
+static int make_tile_map(CUtensorMap *map, const gb_plan *p, const float2 *grid, int box_rows) {
+  const Geom &g = p->g;
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_tiled();
+  if (!fn) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return GB_ERR_CUDA;
+  }
+  const cuuint64_t dims[2] = {(cuuint64_t)g.ngx, (cuuint64_t)g.B * g.NP * (cuuint64_t)g.ngy};
+  const cuuint64_t strides[1] = {(cuuint64_t)g.ngx * sizeof(float2)};
+  const cuuint32_t box[2] = {(cuuint32_t)kCW, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<float2 *>(grid), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed (%d) for a %d x %lld grid batch", (int)r, g.ngx,
+              (long long)dims[1]);
+    return GB_ERR_CUDA;
+  }
+  return GB_OK;
+}
+
+// Kernels whose shared memory exceeds the 48 KB default need the opt-in.
+template <int NP>
+static int setup_np() {
+#define GB_ATTR(K, B) \
+  GB_CUDA(cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(B)))
+  GB_ATTR((k_cols_b_inv<16, NP>), (smem_b_inv<16, NP>()));
+  GB_ATTR((k_cols_b_inv<32, NP>), (smem_b_inv<32, NP>()));
+  GB_ATTR((k_cols_b_inv<64, NP>), (smem_b_inv<64, NP>()));
+  GB_ATTR((k_cols_b_inv<128, NP>), (smem_b_inv<128, NP>()));
+  GB_ATTR((k_cols_b_inv<256, NP>), (smem_b_inv<256, NP>()));
+  GB_ATTR(k_cols_b_pred<256>, smem_one<256>());
+  GB_ATTR((k_cols_a_pred<16, NP>), (smem_a_pred<16, NP>()));
+  GB_ATTR((k_cols_a_pred<32, NP>), (smem_a_pred<32, NP>()));
+  GB_ATTR((k_cols_a_pred<64, NP>), (smem_a_pred<64, NP>()));
+  GB_ATTR((k_cols_a_pred<128, NP>), (smem_a_pred<128, NP>()));
+#undef GB_ATTR
+  return GB_OK;
+}
+
+int setup_col_kernels(gb_plan *p) {
+  if (!p->col_fft) return GB_OK;
+  switch (p->g.NP) {
+    case 1: return setup_np<1>();
+    case 2: return setup_np<2>();
+    default: return setup_np<4>();
+  }
+}
+
 template <int NP>
 static int cols_invert_np(gb_plan *p, float2 *grid, int b0, int nb, float *acc, int first,
                           cudaStream_t s) {
   const Geom &g = p->g;
   const ColGeom cg = col_geom(g);
-  const unsigned tiles = (unsigned)((g.nx + kTC - 1) / kTC);
-  const double *tprime = p->at<double>(p->off_tprime);
-  const double cols = (double)nb * NP * cg.n * g.nx * sizeof(float2);  // central columns
+  const unsigned tiles = (unsigned)((g.nx + kCW - 1) / kCW);
+  const float2 *twn = p->at<float2>(p->off_twn);
+  const ulonglong2 *screen = g.do_w ? p->at<ulonglong2>(p->off_screen) : nullptr;
+  const double cols = (double)nb * NP * cg.n * g.nx * sizeof(float2);  // image columns
   const double npix = (double)g.nx * g.ny;
   {
     ProfScope ps(kProfColInvA, s, 2.0 * cols);
     const dim3 grd(tiles, cg.N2, nb * NP);
-#define GB_COLA(N) k_col_a_inv<N><<<grd, kThreads, 0, s>>>(cg, grid)
+#define GB_COLA(N)                                                                  \
+  k_cols_a_inv<N><<<grd, ColShape<N>::THREADS, smem_one<N>(), s>>>(cg, twn, grid)
     switch (cg.N1) {
       case 16: GB_COLA(16); break;
       case 32: GB_COLA(32); break;
@@ -396,14 +618,20 @@ static int cols_invert_np(gb_plan *p, float2 *grid, int b0, int nb, float *acc, 
       default: GB_COLA(128); break;
     }
 #undef GB_COLA
-    GB_LAUNCH_CHECK("k_col_a_inv");
+    GB_LAUNCH_CHECK("k_cols_a_inv");
   }
   {
     ProfScope ps(kProfColInvB, s,
-                 cols + (first ? 1.0 : 2.0) * sizeof(float) * NP * npix + (g.do_w ? 8.0 * npix : 0.0));
+                 cols + (first ? 1.0 : 2.0) * sizeof(float) * NP * npix +
+                     (g.do_w ? 16.0 * npix : 0.0));
     const dim3 grd(tiles, cg.N1);
-#define GB_COLB(N) \
-  k_col_b_inv<N, NP><<<grd, kThreads, 0, s>>>(cg, g, grid, b0, nb, tprime, acc, first)
+    CUtensorMap map;
+    int rc = make_tile_map(&map, p, grid, cg.N2);
+    if (rc) return rc;
+    uint32_t *status = p->status_word();
+#define GB_COLB(N)                                                                 \
+  k_cols_b_inv<N, NP><<<grd, ColShape<N>::THREADS, smem_b_inv<N, NP>(), s>>>(       \
+      map, cg, twn, screen, g.do_w, b0, nb, acc, first, status)
     switch (cg.N2) {
       case 16: GB_COLB(16); break;
       case 32: GB_COLB(32); break;
@@ -412,7 +640,7 @@ static int cols_invert_np(gb_plan *p, float2 *grid, int b0, int nb, float *acc, 
       default: GB_COLB(256); break;
     }
 #undef GB_COLB
-    GB_LAUNCH_CHECK("k_col_b_inv");
+    GB_LAUNCH_CHECK("k_cols_b_inv");
   }
   return GB_OK;
 }
@@ -422,14 +650,18 @@ static int cols_predict_np(gb_plan *p, const float *img, int b0, int nb, float2 
                            cudaStream_t s) {
   const Geom &g = p->g;
   const ColGeom cg = col_geom(g);
-  const unsigned tiles = (unsigned)((g.nx + kTC - 1) / kTC);
-  const double *tprime = p->at<double>(p->off_tprime);
+  const unsigned tiles = (unsigned)((g.nx + kCW - 1) / kCW);
+  const float2 *twn = p->at<float2>(p->off_twn);
+  const ulonglong2 *screen = g.do_w ? p->at<ulonglong2>(p->off_screen) : nullptr;
   const double cols = (double)nb * NP * cg.n * g.nx * sizeof(float2);
   const double npix = (double)g.nx * g.ny;
   {
-    ProfScope ps(kProfColPredA, s, cols + sizeof(float) * NP * npix + (g.do_w ? 8.0 * npix : 0.0));
-    const dim3 grd(tiles, cg.N2, NP);
-#define GB_COLA(N) k_col_a_pred<N, NP><<<grd, kThreads, 0, s>>>(cg, g, img, tprime, b0, nb, grid)
+    ProfScope ps(kProfColPredA, s,
+                 cols + sizeof(float) * NP * npix + (g.do_w ? 16.0 * npix : 0.0));
+    const dim3 grd(tiles, cg.N2);
+#define GB_COLA(N)                                                                   \
+  k_cols_a_pred<N, NP><<<grd, ColShape<N>::THREADS, smem_a_pred<N, NP>(), s>>>(cg, twn, img, \
+                                                                        screen, g.do_w, b0, nb, grid)
     switch (cg.N1) {
       case 16: GB_COLA(16); break;
       case 32: GB_COLA(32); break;
@@ -437,12 +669,13 @@ static int cols_predict_np(gb_plan *p, const float *img, int b0, int nb, float2 
       default: GB_COLA(128); break;
     }
 #undef GB_COLA
-    GB_LAUNCH_CHECK("k_col_a_pred");
+    GB_LAUNCH_CHECK("k_cols_a_pred");
   }
   {
     ProfScope ps(kProfColPredB, s, 2.0 * cols);
     const dim3 grd(tiles, cg.N1, nb * NP);
-#define GB_COLB(N) k_col_b_pred<N><<<grd, kThreads, 0, s>>>(cg, grid)
+#define GB_COLB(N) \
+  k_cols_b_pred<N><<<grd, ColShape<N>::THREADS, smem_one<N>(), s>>>(cg, twn, grid)
     switch (cg.N2) {
       case 16: GB_COLB(16); break;
       case 32: GB_COLB(32); break;
@@ -451,7 +684,7 @@ static int cols_predict_np(gb_plan *p, const float *img, int b0, int nb, float2 
       default: GB_COLB(256); break;
     }
 #undef GB_COLB
-    GB_LAUNCH_CHECK("k_col_b_pred");
+    GB_LAUNCH_CHECK("k_cols_b_pred");
   }
   {
     // zero the columns outside the image: [0, ox) and [ox + nx, ngx) of every row

@@ -6,6 +6,9 @@
 
 namespace gb {
 
+// Bits of a plan's device status word.
+constexpr uint32_t kErrTmaTimeout = 1u;  // a TMA completion wait ran past its limit
+
 struct ColGeom {
   int n, N1, N2;   // column length n = N1 N2
   int ox, oy;      // image block offset in the grid
@@ -25,11 +28,13 @@ struct RowPerm {
 };
 
 // True when a column of length n has a supported split n = N1 N2
-// (power of two, 256 <= n <= 32768).
+// (power of two, 256 <= n <= 32768; N1 <= 128, N2 <= 256).
 bool column_split(int n, int &N1, int &N2);
 ColGeom col_geom(const Geom &g);
 RowPerm row_perm(const gb_plan *p);
 
+// Shared-memory opt-ins of the column kernels (plan creation).
+int setup_col_kernels(gb_plan *p);
 // Invert: step A in place, then step B fused with the w-screen and the
 // image accumulation (first != 0 starts acc from zero).
 int run_cols_invert(gb_plan *p, void *grid, int b0, int nb, float *acc, int first,

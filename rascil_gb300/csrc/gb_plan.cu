@@ -440,10 +440,17 @@ __global__ void k_slab_items(const uint32_t *__restrict__ offsets, int nslabs, i
 // Correction image [ny][nx]: 1/(phihat_u phihat_v) and, with w-stacking,
 // 1/(phihat_w(dw t') n).  phihat_w by Gauss-Legendre quadrature of the
 // (even) kernel on [0, W/2].
+// frac(x) as 64-bit fixed-point turns (x in turns, FP64).
+__device__ __forceinline__ unsigned long long fixed_turns(double x) {
+  const double f = x - floor(x);  // [0, 1]; 1 wraps to 0 below
+  return ((unsigned long long)(f * 9223372036854775808.0)) << 1;
+}
+
 template <typename R>
 __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
                              const double *__restrict__ cv, const Quad quad,
-                             R *__restrict__ corr, double *__restrict__ tprime) {
+                             R *__restrict__ corr, double *__restrict__ tprime,
+                             ulonglong2 *__restrict__ screen) {
   const int64_t npix = (int64_t)g.nx * g.ny;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npix; i += stride) {
@@ -452,6 +459,11 @@ __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
     if (g.do_w) {
       const double t = pixel_nm1(g, ix, iy);
       tprime[i] = t - g.tc;
+      if (screen) {
+        // plane k sits at w_k = c0 + k dw: phase_k = c0 t' + k (dw t') turns
+        const double c0 = g.w_lo - 0.5 * g.W * g.dw;
+        screen[i] = make_ulonglong2(fixed_turns(c0 * (t - g.tc)), fixed_turns(g.dw * (t - g.tc)));
+      }
       // phihat_w(dw t') by quadrature, in the form's own precision
       const R nu = (R)(g.dw * (t - g.tc));
       R ph = (R)0;
@@ -463,6 +475,16 @@ __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
       f = f / (2.0 * (double)ph * (1.0 + t));
     }
     corr[i] = (R)f;
+  }
+}
+
+// exp(+2 pi i m / n), m < n, rounded from FP64.
+__global__ void k_twiddles(int n, float2 *__restrict__ tw) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < n) {
+    double sn, cs;
+    sincospi(2.0 * (double)m / (double)n, &sn, &cs);
+    tw[m] = make_float2((float)cs, (float)sn);
   }
 }
 
@@ -573,14 +595,16 @@ static int make_fft(gb_plan *p, int planes, cufftHandle *h, size_t *work) {
 // Column mode applies to the FP32 form with a power-of-two grid height.
 static int choose_fft_mode(gb_plan *p) {
   int n1, n2;
-  const bool fits = p->precision == GB_FP32 && column_split(p->g.ngy, n1, n2);
+  const bool fits = p->precision == GB_FP32 && p->g.ngy == 2 * p->g.ny &&
+                    (p->g.ngx - p->g.nx) % 4 == 0 && column_split(p->g.ngy, n1, n2);
   switch (p->params.fft_mode) {
     case GB_FFT_AUTO: p->col_fft = fits; return GB_OK;
     case GB_FFT_CUFFT_2D: p->col_fft = false; return GB_OK;
     case GB_FFT_COLUMNS:
       if (!fits) {
-        set_error("fft_mode GB_FFT_COLUMNS needs the FP32 form and a power-of-two grid height "
-                  "in [256, 32768] (grid %d x %d)", p->g.ngx, p->g.ngy);
+        set_error("fft_mode GB_FFT_COLUMNS needs the FP32 form, a grid height of twice the "
+                  "image height, a power of two in [256, 32768], and an even column offset "
+                  "(grid %d x %d, image %d x %d)", p->g.ngx, p->g.ngy, p->g.nx, p->g.ny);
         return GB_ERR_INVALID_ARG;
       }
       p->col_fft = true;
@@ -610,6 +634,10 @@ static int layout_workspace(gb_plan *p) {
   off = align_up(off + rb * (size_t)g.nx * g.ny);
   p->off_tprime = off;
   off = align_up(off + (g.do_w ? 8 * (size_t)g.nx * g.ny : 0));
+  p->off_screen = off;
+  off = align_up(off + (p->col_fft && g.do_w ? 16 * (size_t)g.nx * g.ny : 0));
+  p->off_twn = off;
+  off = align_up(off + (p->col_fft ? 8 * (size_t)g.ngy : 0));
   p->off_tables = off;
   off = align_up(off + 8 * ((size_t)g.nx + g.ny + 2 * kMaxQuad));
   p->off_counters = off;
@@ -667,6 +695,7 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
       (nb + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
   const double ni = (double)g.nitems, rows = (double)g.R * 24.0 + 8.0 * g.C;
   GB_CUDA(cudaMemsetAsync(counts, 0, 4 * (size_t)(nb + 1), s));
+  GB_CUDA(cudaMemsetAsync(p->status_word(), 0, 4, s));
   {
     ProfScope ps(kProfCountKernel, s, rows + 8.0 * ni);
     k_count<<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, counts, keys, ranks);
@@ -714,9 +743,15 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
                                                           (int64_t)p->num_sms * 32);
   {
     ProfScope ps(kProfCorr, s, (double)npix * (sizeof(R) + (g.do_w ? 8.0 : 0.0)));
+    ulonglong2 *screen = p->col_fft && g.do_w ? p->at<ulonglong2>(p->off_screen) : nullptr;
     k_corr_image<R><<<pix_blocks, kThreads, 0, s>>>(g, cu, cv, p->quad, p->at<R>(p->off_corr),
-                                                     p->at<double>(p->off_tprime));
+                                                     p->at<double>(p->off_tprime), screen);
     GB_LAUNCH_CHECK("k_corr_image");
+  }
+  if (p->col_fft) {
+    k_twiddles<<<(g.ngy + kThreads - 1) / kThreads, kThreads, 0, s>>>(g.ngy,
+                                                                     p->at<float2>(p->off_twn));
+    GB_LAUNCH_CHECK("k_twiddles");
   }
   return GB_OK;
 }
@@ -900,6 +935,7 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
   p->fft_work_bytes = std::max<size_t>(std::max(w_full, w_rem), 4096);
   layout_workspace(p);
   rc = setup_tile_kernels(p);
+  if (!rc) rc = setup_col_kernels(p);
   if (rc) {
     gb_plan_destroy(p);
     return rc;
@@ -1001,6 +1037,24 @@ int gb_plan_export_items(const gb_plan *p, uint32_t *bucket_dev, int32_t *cell_d
         p->g, p->at<ItemF>(p->off_items), p->at<Chunk>(p->off_chunks),
         p->at<uint32_t>(p->off_chunk_off), bucket_dev, cell_dev, frac_dev);
   GB_LAUNCH_CHECK("k_export_items");
+  return GB_OK;
+}
+
+int gb_plan_device_status(gb_plan *p, void *stream, int32_t *status_out) {
+  if (!p || !status_out) {
+    set_error("gb_plan_device_status: NULL argument");
+    return GB_ERR_INVALID_ARG;
+  }
+  if (!p->bound) {
+    set_error("gb_plan_device_status: plan is not bound");
+    return GB_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t v = 0;
+  GB_CUDA(cudaMemcpyAsync(&v, p->status_word(), 4, cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaMemsetAsync(p->status_word(), 0, 4, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  *status_out = (int32_t)v;
   return GB_OK;
 }
 

@@ -40,6 +40,9 @@ struct gb_plan {
   // column transforms are the library's own kernels (gb_fft.cu)
   bool col_fft = false;
   size_t off_tprime = 0;  // [ny][nx] float64: n - 1 - tc per pixel (w-stacking)
+  // column mode: [ny][nx] w-screen phases as 64-bit fixed-point turns
+  // (A, D), plane k's phase = A + k D mod 1; [ngy] exp(+2 pi i m / ngy)
+  size_t off_screen = 0, off_twn = 0;
   bool bound = false;
   bool owns_ws = false;
   cudaStream_t last_stream = nullptr;
@@ -55,6 +58,9 @@ struct gb_plan {
     if (slab_items.empty() || s_lo > s_hi) return 0;
     return slab_items[s_hi + 1] - slab_items[s_lo];
   }
+
+  // Device status word (kernels OR error bits in; gb_plan_device_status reads it).
+  uint32_t *status_word() const { return at<uint32_t>(off_counters) + 2 * nbatches; }
 
   template <typename T> T *at(size_t off) const {
     return reinterpret_cast<T *>(ws + off);

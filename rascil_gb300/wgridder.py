@@ -231,6 +231,17 @@ class Plan:
                                             _stream(self.device)), "gb_plan_dirty2ms")
         return out
 
+    def device_status(self):
+        """Error bits the plan's kernels recorded since the last call (0 =
+        none; 1 = a TMA completion wait hit its limit, so that call's output
+        is invalid), then cleared.  Waits for the current stream."""
+        v = ctypes.c_int32()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().gb_plan_device_status(self._handle, _stream(self.device),
+                                                         ctypes.byref(v)),
+                       "gb_plan_device_status")
+        return int(v.value)
+
     def close(self):
         if getattr(self, "_handle", None) is not None and self._handle.value:
             _lib.load().gb_plan_destroy(self._handle)

@@ -66,6 +66,7 @@ def test_invert_predict_vs_dft(do_w, nx, ny):
     vis = p.dirty2ms(_dev(img[None], torch.float32), layout="xy")[..., 0].cpu().numpy()
     vref = dft.dirty2ms_dft(c["uvw"], c["freq"], img, None, c["pixsize"], c["pixsize"], do_w)
     assert rel_rms(vis, vref) < TOL
+    assert p.device_status() == 0
     p.close()
 
 
@@ -91,6 +92,7 @@ def test_tall_images_vs_fp64(nx, ny):
     v32 = pf.dirty2ms(_dev(img, torch.float32)).cpu().numpy()
     v64 = pd.dirty2ms(_dev(img, torch.float64)).cpu().numpy()
     assert rel_rms(v32, v64) < TOL
+    assert pf.device_status() == 0
     pf.close()
     pd.close()
 
@@ -112,6 +114,7 @@ def test_multi_pol_and_batches(npol):
     v32 = pc.dirty2ms(_dev(c["img"], torch.float32)).cpu().numpy()
     v64 = pd.dirty2ms(_dev(c["img"], torch.float64)).cpu().numpy()
     assert rel_rms(v32, v64) < TOL
+    assert pc.device_status() == 0
     pc.close()
     pd.close()
 
@@ -129,5 +132,6 @@ def test_modes_agree():
     assert rel_rms(da, db) < 2e-6
     img = _dev(c["img"], torch.float32)
     assert rel_rms(a.dirty2ms(img).cpu().numpy(), b.dirty2ms(img).cpu().numpy()) < 2e-6
+    assert a.device_status() == 0
     a.close()
     b.close()
