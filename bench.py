@@ -65,6 +65,8 @@ def parse():
                     help="memory for one batch of w-planes (0 = planner default)")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the per-shape autotuner (use cached or default plan parameters)")
+    ap.add_argument("--plan", default=None,
+                    help="fixed plan parameters sigma,tile,slab (e.g. 2,16,2); implies --no-tune")
     ap.add_argument("--fft-mode", default="auto", choices=["auto", "columns", "cufft2d"],
                     help="per-plane transforms of the FP32 form (auto: column kernels where "
                          "they apply)")
@@ -198,11 +200,12 @@ class Workload:
 
 GRID_BUDGET = [0]
 FFT_MODE = ["auto"]
+FIXED_PLAN = [None]
 
 
 def make_plan(wl, precision, params=None):
     from rascil_gb300.wgridder import Plan
-    params = params or {}
+    params = params or FIXED_PLAN[0] or {}
     return Plan(wl.uvw, wl.freq_dev, wl.npixel, wl.npixel, wl.cell, wl.cell, wl.epsilon, True,
                 npol=wl.npol, precision=precision, grid_budget_bytes=GRID_BUDGET[0],
                 sigma=params.get("sigma", 0.0), tile=params.get("tile", 0),
@@ -474,6 +477,10 @@ def main():
     import torch
     GRID_BUDGET[0] = int(args.grid_budget_gb * (1 << 30))
     FFT_MODE[0] = args.fft_mode
+    if args.plan:
+        sg, tl, sb = args.plan.split(",")
+        FIXED_PLAN[0] = {"sigma": float(sg), "tile": int(tl), "slab": int(sb)}
+        args.no_tune = True
     rank, world = dist_setup(args)
     device = torch.device("cuda", torch.cuda.current_device())
     from rascil_gb300 import _lib

@@ -53,11 +53,12 @@ typedef enum { GB_FP32 = 0, GB_FP64 = 1 } gb_precision;
 
 /* How the per-plane 2-D transforms run.  GB_FFT_AUTO picks
  * GB_FFT_COLUMNS where it applies (FP32 form, grid height a power of two
- * from 256 to 32768), else GB_FFT_CUFFT_2D.  GB_FFT_COLUMNS: batched 1-D
- * cuFFT rows plus the library's own column kernels, pruned to the image's
- * columns and fused with the w-screen (asking for it where it does not
- * apply is GB_ERR_INVALID_ARG).  GB_FFT_CUFFT_2D: batched 2-D cuFFT plans
- * plus separate screen passes. */
+ * from 256 to 32768, twice the image height, even column offset), else
+ * GB_FFT_CUFFT_2D.  GB_FFT_COLUMNS: the library's own column kernels,
+ * pruned to the image's columns and fused with the w-screen, with its own
+ * row kernels for grid widths 4096, 8192 and 16384 (else batched 1-D cuFFT
+ * rows); asking for it where it does not apply is GB_ERR_INVALID_ARG.
+ * GB_FFT_CUFFT_2D: batched 2-D cuFFT plans plus separate screen passes. */
 typedef enum { GB_FFT_AUTO = 0, GB_FFT_CUFFT_2D = 1, GB_FFT_COLUMNS = 2 } gb_fft_mode;
 
 /* Image memory layout.  GB_LAYOUT_XY is ducc0's dirty[x][y] (what
@@ -95,6 +96,9 @@ typedef struct {
   double beta, sigma, dw, w_lo, w_hi, tc;
   int64_t nitems, nbuckets, workspace_bytes;
   int32_t fft_mode;    /* the gb_fft_mode in use (never GB_FFT_AUTO)           */
+  int32_t own_rows;    /* 1: GB_FFT_COLUMNS with the library's row transforms
+                          (grid width 4096, 8192 or 16384: no cuFFT plan, rows
+                          without visibilities skipped); 0: cuFFT rows      */
 } gb_plan_info;
 
 typedef struct gb_plan gb_plan;

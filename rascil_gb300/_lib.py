@@ -77,6 +77,7 @@ class PlanInfo(_c.Structure):
         ("nbuckets", _c.c_int64),
         ("workspace_bytes", _c.c_int64),
         ("fft_mode", _c.c_int32),
+        ("own_rows", _c.c_int32),
     ]
 
     def as_dict(self):

@@ -43,6 +43,7 @@
 
 #include <mutex>
 
+#include "gb_async.cuh"
 #include "gb_fft.cuh"
 
 namespace gb {
@@ -131,10 +132,33 @@ template <int S> __device__ __forceinline__ void dft16(float2 *a) {
   }
 }
 
+// cos / sin(2 pi k / 32), k < 16
+__device__ __constant__ float kCos32[16] = {1.0f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254524f, 0.70710678118654757f, 0.55557023301960229f, 0.38268343236508984f, 0.19509032201612833f, 0.0f, -0.19509032201612819f, -0.38268343236508973f, -0.55557023301960196f, -0.70710678118654746f, -0.83146961230254535f, -0.92387953251128674f, -0.98078528040323043f};
+__device__ __constant__ float kSin32[16] = {0.0f, 0.19509032201612825f, 0.38268343236508978f, 0.55557023301960218f, 0.70710678118654746f, 0.83146961230254524f, 0.92387953251128674f, 0.98078528040323043f, 1.0f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254546f, 0.70710678118654757f, 0.55557023301960218f, 0.38268343236508989f, 0.19509032201612861f};
+
+// 32 = 2 x 16: X[k] = E[k] + w^k O[k], X[k + 16] = E[k] - w^k O[k].
+template <int S> __device__ __forceinline__ void dft32(float2 *a) {
+  float2 e[16], o[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    e[i] = a[2 * i];
+    o[i] = a[2 * i + 1];
+  }
+  dft16<S>(e);
+  dft16<S>(o);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const float2 t = k == 0 ? o[0] : cmulc(o[k], kCos32[k], S * kSin32[k]);
+    a[k] = cadd(e[k], t);
+    a[k + 16] = csub(e[k], t);
+  }
+}
+
 template <int L, int S> __device__ __forceinline__ void dft(float2 *a) {
   if constexpr (L == 4) dft4<S>(a);
   else if constexpr (L == 8) dft8<S>(a);
-  else dft16<S>(a);
+  else if constexpr (L == 16) dft16<S>(a);
+  else dft32<S>(a);
 }
 
 // N-point DFT of every column of a tile.  On entry x[m] holds column
@@ -179,60 +203,6 @@ __device__ __forceinline__ void screen_sincos(ulonglong2 ad, int k, float *sn, f
   const unsigned long long ph = ad.x + (unsigned long long)(unsigned)k * ad.y;
   const int hi = (int)(unsigned)(ph >> 32);  // turns * 2^32 in [-2^31, 2^31)
   sincospif((float)hi * 0x1p-31f, sn, cs);
-}
-
-__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gmem_src, bool valid) {
-  const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(gmem_src),
-               "r"(valid ? 8 : 0)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
-// TMA (bulk tensor copies) with mbarrier completion.
-__device__ __forceinline__ unsigned smem_u32(const void *p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void fence_mbarrier_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
-                                            uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
-      "{%2, %3}], [%4];\n" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
-  unsigned done;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(done)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-// Bounded wait for the phase with the given parity to complete.
-constexpr int kMbarSpins = 1 << 20;
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
-  for (int i = 0; i < kMbarSpins; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
 }
 
 // ----------------------------------------------------------------------
@@ -472,6 +442,120 @@ __global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 3)
 }
 
 // ----------------------------------------------------------------------
+// Row transforms (both forms of the pass over contiguous rows), one CTA
+// per row with the whole row in shared memory.  N = R1 R2 R3 by two nested
+// four-step splits (all in registers, two shared-memory exchanges):
+//   pass 1  unit t < R2 R3 holds x[t + R2 R3 m], m < R1: R1-point DFT,
+//           times w_N^(t k1);
+//   pass 2  unit (k1, s), s < R3, holds the pass-1 outputs k1 of units
+//           s + R3 m': R2-point DFT, times w_(R2 R3)^(s k1');
+//   pass 3  unit (k1, k1') holds the pass-2 outputs k1' of units (k1, s):
+//           R3-point DFT, giving X[k1 + R1 k1' + R1 R2 k2'].
+// Input columns outside [in_lo, in_hi) are taken as zero (predict: only the
+// image columns hold data) and only outputs in [out_lo, out_hi) are stored
+// (invert: only the image columns are needed).  Rows whose (plane, row
+// tile) is empty in the occupancy mask are skipped: an invert row there is
+// zero (nothing gridded), a predict row there is never degridded.
+template <int N> struct RowShape;
+template <> struct RowShape<16384> {
+  static constexpr int R1 = 32, R2 = 32, R3 = 16, THREADS = 512, MINB = 1;
+};
+template <> struct RowShape<8192> {
+  static constexpr int R1 = 32, R2 = 16, R3 = 16, THREADS = 256, MINB = 2;
+};
+template <> struct RowShape<4096> {
+  static constexpr int R1 = 32, R2 = 16, R3 = 8, THREADS = 128, MINB = 4;
+};
+
+struct RowArgs {
+  float2 *grid;              // batch buffer: rows of ngx cells
+  const uint8_t *mask;       // [nplanes][ntv] occupancy, or null
+  const float2 *twx;         // exp(+2 pi i m / ngx), m < ngx
+  int64_t nrows;             // nb NP ngy rows in this batch
+  int ngy, NP, b0, T, ntv;
+  int perm_s1, perm_s2;      // predict rows: logical row of physical r, or -1
+  int in_lo, in_hi, out_lo, out_hi;
+};
+
+template <int N, int S>
+__global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
+    k_rows(const RowArgs ra) {
+  using RS = RowShape<N>;
+  constexpr int R1 = RS::R1, R2 = RS::R2, R3 = RS::R3, TH = RS::THREADS;
+  constexpr int TN = R2 * R3;  // pass-1 units
+  constexpr int NA = N / 128;  // two-level twiddle table: w^m = A[m >> 7] B[m & 127]
+  static_assert(TN == TH, "one pass-1 unit per thread");
+  extern __shared__ __align__(16) float2 smem[];
+  float2 *ex = smem;                        // exchange: max(R1 (TN + 1), N) cells
+  float2 *ta = smem + R1 * (TN + 1);        // [NA]
+  float2 *tb = ta + NA;                     // [128]
+  for (int i = threadIdx.x; i < NA + 128; i += TH) {
+    const float2 w = ra.twx[i < NA ? i * 128 : i - NA];
+    (i < NA ? ta[i] : tb[i - NA]) = S > 0 ? w : conjf2(w);
+  }
+  __syncthreads();
+  auto tw = [&](int m) { return cmul(ta[m >> 7], tb[m & 127]); };
+  const int t = threadIdx.x;
+  for (int64_t row = blockIdx.x; row < ra.nrows; row += gridDim.x) {
+    if (ra.mask) {
+      const int sp = (int)(row / ra.ngy), r = (int)(row - (int64_t)sp * ra.ngy);
+      const int q = ra.perm_s1 < 0 ? r
+                                   : (r >> ra.perm_s2) + ((r & ((1 << ra.perm_s2) - 1)) << ra.perm_s1);
+      const int k = ra.b0 + sp / ra.NP;
+      if (!ra.mask[(int64_t)k * ra.ntv + q / ra.T]) continue;  // uniform over the CTA
+    }
+    float2 *rp = ra.grid + row * N;
+    // pass 1
+    float2 x[R1];
+#pragma unroll
+    for (int m = 0; m < R1; ++m) {
+      const int col = t + TN * m;
+      x[m] = (col >= ra.in_lo && col < ra.in_hi) ? rp[col] : make_float2(0.f, 0.f);
+    }
+    dft<R1, S>(x);
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) ex[k1 * (TN + 1) + t] = k1 ? cmul(x[k1], tw(t * k1)) : x[k1];
+    __syncthreads();
+    // pass 2: units u = k1 + R1 s
+    constexpr int U2 = R1 * R3 / TH;
+    float2 y[U2][R2];
+#pragma unroll
+    for (int i = 0; i < U2; ++i) {
+      const int u = t + TH * i, k1 = u % R1, s = u / R1;
+#pragma unroll
+      for (int m = 0; m < R2; ++m) y[i][m] = ex[k1 * (TN + 1) + s + R3 * m];
+      dft<R2, S>(y[i]);
+#pragma unroll
+      for (int k = 1; k < R2; ++k) y[i][k] = cmul(y[i][k], tw(s * k * R1));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < U2; ++i) {
+      const int u = t + TH * i, k1 = u % R1, s = u / R1;
+#pragma unroll
+      for (int k = 0; k < R2; ++k) ex[(k * R3 + s) * R1 + k1] = y[i][k];
+    }
+    __syncthreads();
+    // pass 3: units u = k1 + R1 k1'
+    constexpr int U3 = R1 * R2 / TH;
+#pragma unroll
+    for (int i = 0; i < U3; ++i) {
+      const int u = t + TH * i, k1 = u % R1, kp = u / R1;
+      float2 z[R3];
+#pragma unroll
+      for (int s = 0; s < R3; ++s) z[s] = ex[(kp * R3 + s) * R1 + k1];
+      dft<R3, S>(z);
+#pragma unroll
+      for (int k2 = 0; k2 < R3; ++k2) {
+        const int o = k1 + R1 * kp + R1 * R2 * k2;
+        if (o >= ra.out_lo && o < ra.out_hi) rp[o] = z[k2];
+      }
+    }
+    __syncthreads();  // exchange slots free for the next row
+  }
+}
+
+// ----------------------------------------------------------------------
 // host side
 
 static int ilog2(int n) {
@@ -686,14 +770,92 @@ static int cols_predict_np(gb_plan *p, const float *img, int b0, int nb, float2 
 #undef GB_COLB
     GB_LAUNCH_CHECK("k_cols_b_pred");
   }
-  {
+  if (!p->row_fft) {
     // zero the columns outside the image: [0, ox) and [ox + nx, ngx) of every row
+    // (k_rows reads only the image columns, so it needs no zeros there)
     const size_t rows = (size_t)nb * NP * g.ngy, pitch = sizeof(float2) * g.ngx;
     const size_t left = sizeof(float2) * cg.ox, right = sizeof(float2) * (g.ngx - cg.ox - g.nx);
     ProfScope ps(kProfZeroMargins, s, (double)rows * (left + right));
     if (left) GB_CUDA(cudaMemset2DAsync(grid, pitch, 0, left, rows, s));
     if (right) GB_CUDA(cudaMemset2DAsync(grid + cg.ox + g.nx, pitch, 0, right, rows, s));
   }
+  return GB_OK;
+}
+
+bool row_kernel_fits(int n) { return n == 4096 || n == 8192 || n == 16384; }
+
+template <int N> constexpr size_t rows_smem() {
+  using RS = RowShape<N>;
+  return sizeof(float2) * ((size_t)RS::R1 * (RS::R2 * RS::R3 + 1) + N / 128 + 128);
+}
+
+template <int N, int S> static int rows_occupancy(int *per_sm) {
+  GB_CUDA(cudaFuncSetAttribute(k_rows<N, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)rows_smem<N>()));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_rows<N, S>,
+                                                        RowShape<N>::THREADS, rows_smem<N>()));
+  return GB_OK;
+}
+
+int setup_row_kernels(gb_plan *p) {
+  if (!p->row_fft) return GB_OK;
+  int a = 0, b = 0, rc;
+  switch (p->g.ngx) {
+    case 4096: rc = rows_occupancy<4096, 1>(&a); if (!rc) rc = rows_occupancy<4096, -1>(&b); break;
+    case 8192: rc = rows_occupancy<8192, 1>(&a); if (!rc) rc = rows_occupancy<8192, -1>(&b); break;
+    default: rc = rows_occupancy<16384, 1>(&a); if (!rc) rc = rows_occupancy<16384, -1>(&b); break;
+  }
+  if (rc) return rc;
+  if (std::min(a, b) < 1) {
+    set_error("k_rows cannot launch for rows of %d cells", p->g.ngx);
+    return GB_ERR_INVALID_ARG;
+  }
+  p->row_blocks = std::min(a, b) * p->num_sms;
+  return GB_OK;
+}
+
+int run_rows(gb_plan *p, void *grid, int b0, int nb, int dir, cudaStream_t s) {
+  const Geom &g = p->g;
+  const ColGeom cg = col_geom(g);
+  RowArgs ra;
+  ra.grid = reinterpret_cast<float2 *>(grid);
+  ra.mask = p->at<uint8_t>(p->off_rowmask);
+  ra.twx = p->at<float2>(p->off_twx);
+  ra.nrows = (int64_t)nb * g.NP * g.ngy;
+  ra.ngy = g.ngy;
+  ra.NP = g.NP;
+  ra.b0 = b0;
+  ra.T = g.T;
+  ra.ntv = g.ntv;
+  if (dir > 0) {  // invert: full rows in, image columns out
+    ra.perm_s1 = -1;
+    ra.perm_s2 = 0;
+    ra.in_lo = 0;
+    ra.in_hi = g.ngx;
+    ra.out_lo = cg.ox;
+    ra.out_hi = cg.ox + g.nx;
+  } else {  // predict: image columns in (rest taken as zero), full rows out
+    const RowPerm rp = row_perm(p);
+    ra.perm_s1 = rp.s1;
+    ra.perm_s2 = rp.s2;
+    ra.in_lo = cg.ox;
+    ra.in_hi = cg.ox + g.nx;
+    ra.out_lo = 0;
+    ra.out_hi = g.ngx;
+  }
+  const unsigned blocks = (unsigned)std::min<int64_t>(p->row_blocks, ra.nrows);
+#define GB_ROWS(N)                                                                        \
+  if (dir > 0)                                                                            \
+    k_rows<N, 1><<<blocks, RowShape<N>::THREADS, rows_smem<N>(), s>>>(ra);                \
+  else                                                                                    \
+    k_rows<N, -1><<<blocks, RowShape<N>::THREADS, rows_smem<N>(), s>>>(ra);
+  switch (g.ngx) {
+    case 4096: GB_ROWS(4096) break;
+    case 8192: GB_ROWS(8192) break;
+    default: GB_ROWS(16384) break;
+  }
+#undef GB_ROWS
+  GB_LAUNCH_CHECK("k_rows");
   return GB_OK;
 }
 

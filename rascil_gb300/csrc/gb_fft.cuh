@@ -35,6 +35,15 @@ RowPerm row_perm(const gb_plan *p);
 
 // Shared-memory opt-ins of the column kernels (plan creation).
 int setup_col_kernels(gb_plan *p);
+// Row lengths with a k_rows instantiation (4096, 8192, 16384).
+bool row_kernel_fits(int n);
+// Occupancy / opt-ins of the row kernels (plan creation).
+int setup_row_kernels(gb_plan *p);
+// Row transforms of nb planes x NP pols of the batch buffer: dir > 0
+// invert (e^{+}, full rows in, image columns out), dir < 0 predict (e^{-},
+// image columns in, full rows out); rows empty in the occupancy mask are
+// skipped.
+int run_rows(gb_plan *p, void *grid, int b0, int nb, int dir, cudaStream_t s);
 // Invert: step A in place, then step B fused with the w-screen and the
 // image accumulation (first != 0 starts acc from zero).
 int run_cols_invert(gb_plan *p, void *grid, int b0, int nb, float *acc, int first,

@@ -449,7 +449,10 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
       GB_LAUNCH_CHECK("k_grid");
     }
     int rc;
-    {
+    if (p->row_fft) {
+      ProfScope ps(kProfRowsInv, s, 1.5 * gbytes);
+      rc = run_rows(p, grid, b0, nb, 1, s);
+    } else {
       ProfScope ps(kProfFftInv, s, 2.0 * gbytes);
       rc = run_fft(p, nb, grid, CUFFT_INVERSE, s);
     }

@@ -478,6 +478,28 @@ __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,
   }
 }
 
+// Occupancy of (w-plane, row tile): a chunk's items reach planes
+// [slab S, slab S + S + W - 1) and rows [tv T, tv T + T + W - 1) (mod ngy).
+__global__ void k_row_mask(const Geom g, const Chunk *__restrict__ chunks,
+                           const uint32_t *__restrict__ chunk_off, uint8_t *__restrict__ mask) {
+  const uint32_t nch = chunk_off[g.nbuckets];
+  const int ntiles = g.ntu * g.ntv;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nch; c += gridDim.x * blockDim.x) {
+    const uint32_t bucket = chunks[c].bucket;
+    const int slab = (int)(bucket / (uint32_t)ntiles);
+    const int tv = (int)(bucket - (uint32_t)slab * ntiles) / g.ntu;
+    const int k_lo = slab * g.S, k_hi = min(k_lo + g.S + g.W - 1, g.nplanes);
+    const int r_lo = tv * g.T, r_hi = tv * g.T + g.T + g.W - 2;  // inclusive
+    for (int k = k_lo; k < k_hi; ++k) {
+      for (int r = r_lo; r <= r_hi + g.T - 1; r += g.T) {
+        int rr = min(r, r_hi);
+        while (rr >= g.ngy) rr -= g.ngy;
+        mask[(int64_t)k * g.ntv + rr / g.T] = 1;
+      }
+    }
+  }
+}
+
 // exp(+2 pi i m / n), m < n, rounded from FP64.
 __global__ void k_twiddles(int n, float2 *__restrict__ tw) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -598,8 +620,8 @@ static int choose_fft_mode(gb_plan *p) {
   const bool fits = p->precision == GB_FP32 && p->g.ngy == 2 * p->g.ny &&
                     (p->g.ngx - p->g.nx) % 4 == 0 && column_split(p->g.ngy, n1, n2);
   switch (p->params.fft_mode) {
-    case GB_FFT_AUTO: p->col_fft = fits; return GB_OK;
-    case GB_FFT_CUFFT_2D: p->col_fft = false; return GB_OK;
+    case GB_FFT_AUTO: p->col_fft = fits; break;
+    case GB_FFT_CUFFT_2D: p->col_fft = false; break;
     case GB_FFT_COLUMNS:
       if (!fits) {
         set_error("fft_mode GB_FFT_COLUMNS needs the FP32 form, a grid height of twice the "
@@ -608,11 +630,13 @@ static int choose_fft_mode(gb_plan *p) {
         return GB_ERR_INVALID_ARG;
       }
       p->col_fft = true;
-      return GB_OK;
+      break;
     default:
       set_error("unknown fft_mode %d", p->params.fft_mode);
       return GB_ERR_INVALID_ARG;
   }
+  p->row_fft = p->col_fft && row_kernel_fits(p->g.ngx);
+  return GB_OK;
 }
 
 static int layout_workspace(gb_plan *p) {
@@ -638,6 +662,10 @@ static int layout_workspace(gb_plan *p) {
   off = align_up(off + (p->col_fft && g.do_w ? 16 * (size_t)g.nx * g.ny : 0));
   p->off_twn = off;
   off = align_up(off + (p->col_fft ? 8 * (size_t)g.ngy : 0));
+  p->off_twx = off;
+  off = align_up(off + (p->row_fft ? 8 * (size_t)g.ngx : 0));
+  p->off_rowmask = off;
+  off = align_up(off + (p->row_fft ? (size_t)g.nplanes * g.ntv : 0));
   p->off_tables = off;
   off = align_up(off + 8 * ((size_t)g.nx + g.ny + 2 * kMaxQuad));
   p->off_counters = off;
@@ -753,6 +781,17 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
                                                                      p->at<float2>(p->off_twn));
     GB_LAUNCH_CHECK("k_twiddles");
   }
+  if (p->row_fft) {
+    k_twiddles<<<(g.ngx + kThreads - 1) / kThreads, kThreads, 0, s>>>(g.ngx,
+                                                                     p->at<float2>(p->off_twx));
+    GB_LAUNCH_CHECK("k_twiddles");
+    uint8_t *mask = p->at<uint8_t>(p->off_rowmask);
+    GB_CUDA(cudaMemsetAsync(mask, 0, (size_t)g.nplanes * g.ntv, s));
+    const unsigned cb = (unsigned)std::min<int64_t>(
+        ((int64_t)p->max_chunks + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
+    k_row_mask<<<cb, kThreads, 0, s>>>(g, chunks, chunk_off, mask);
+    GB_LAUNCH_CHECK("k_row_mask");
+  }
   return GB_OK;
 }
 
@@ -835,6 +874,7 @@ int gb_plan_geometry(const gb_plan_params *params, double w_lo, double w_hi,
   info->nbuckets = g.nbuckets;
   info->workspace_bytes = (int64_t)tmp.ws_bytes;
   info->fft_mode = tmp.col_fft ? GB_FFT_COLUMNS : GB_FFT_CUFFT_2D;
+  info->own_rows = tmp.row_fft ? 1 : 0;
   return GB_OK;
 }
 
@@ -914,14 +954,16 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
     gb_plan_destroy(p);
     return rc;
   }
-  rc = make_fft(p, p->g.B, &p->fft_full, &w_full);
-  if (rc) {
-    gb_plan_destroy(p);
-    return rc;
-  }
-  p->fft_full_ok = true;
   p->rem_planes = p->g.nplanes % p->g.B;
-  if (p->rem_planes) {
+  if (!p->row_fft) {
+    rc = make_fft(p, p->g.B, &p->fft_full, &w_full);
+    if (rc) {
+      gb_plan_destroy(p);
+      return rc;
+    }
+    p->fft_full_ok = true;
+  }
+  if (p->rem_planes && !p->row_fft) {
     rc = make_fft(p, p->rem_planes, &p->fft_rem, &w_rem);
     if (rc) {
       gb_plan_destroy(p);
@@ -936,6 +978,7 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
   layout_workspace(p);
   rc = setup_tile_kernels(p);
   if (!rc) rc = setup_col_kernels(p);
+  if (!rc) rc = setup_row_kernels(p);
   if (rc) {
     gb_plan_destroy(p);
     return rc;
@@ -1013,6 +1056,7 @@ int gb_plan_info_get(const gb_plan *p, gb_plan_info *info) {
   info->nbuckets = g.nbuckets;
   info->workspace_bytes = (int64_t)p->ws_bytes;
   info->fft_mode = p->col_fft ? GB_FFT_COLUMNS : GB_FFT_CUFFT_2D;
+  info->own_rows = p->row_fft ? 1 : 0;
   return GB_OK;
 }
 

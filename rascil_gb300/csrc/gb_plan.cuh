@@ -39,6 +39,11 @@ struct gb_plan {
   // column mode (FP32): the plans above are 1-D row transforms and the
   // column transforms are the library's own kernels (gb_fft.cu)
   bool col_fft = false;
+  // column mode with rows of 4096 / 8192 / 16384 cells: the row transforms
+  // are k_rows too (no cuFFT plan), with a (plane, row tile) occupancy mask
+  bool row_fft = false;
+  size_t off_rowmask = 0, off_twx = 0;
+  int row_blocks = 0;
   size_t off_tprime = 0;  // [ny][nx] float64: n - 1 - tc per pixel (w-stacking)
   // column mode: [ny][nx] w-screen phases as 64-bit fixed-point turns
   // (A, D), plane k's phase = A + k D mod 1; [ngy] exp(+2 pi i m / ngy)

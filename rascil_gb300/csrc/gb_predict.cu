@@ -19,6 +19,7 @@
 //                           item) or accumulates (later batches) in place.
 #include <cufft.h>
 
+#include "gb_async.cuh"
 #include "gb_fft.cuh"
 #include "gb_plan.cuh"
 
@@ -131,7 +132,6 @@ __global__ void __launch_bounds__(kThreads)
   const int ntiles = g.ntu * g.ntv;
   const int64_t plane = (int64_t)g.ngx * g.ngy;
   const int wk = g.do_w ? W : 1;
-  const int nrow_steps = (W + LM::RS - 1) / LM::RS;
   const int lo = b0 - (g.S + W - 2);
   const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
   const int s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
@@ -201,7 +201,9 @@ __global__ void __launch_bounds__(kThreads)
           sr[q] = (R)0;
           si[q] = (R)0;
         }
-        for (int r = 0; r < nrow_steps; ++r) {
+        constexpr int kMaxRows = (AW + LM::RS - 1) / LM::RS;  // W <= AW: unrolled, predicated
+#pragma unroll
+        for (int r = 0; r < kMaxRows; ++r) {
           const int b = lm.r0 + r * LM::RS;
           const R kv = __shfl_sync(0xffffffffu, kv_lane, 16 + min(b, W - 1));
           if (b < W && lm.a < W) {
@@ -310,6 +312,261 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// FP32 degridder, one item per thread.  A CTA takes a chunk (up to 256
+// items of one bucket); thread i owns item i: its u and v kernel values
+// (with the checkerboard sign (-1)^(p+q) folded in) stay in registers for
+// all planes, and for every plane the thread sums its whole W x W footprint
+// from the plane's staged sub-grid ([SW][pitch][NP] complex, a cell's pols
+// contiguous), double-buffered with cp.async so plane k + 1 streams in
+// while plane k is summed.
+// Per item-plane that is W^2 NP shared loads and 2 W^2 NP FMAs with no
+// cross-lane reduction, against the warp-per-item map of k_degrid.
+template <int NP, int WT>
+__global__ void __launch_bounds__(kThreads, 2)
+    k_degrid_lane(const Geom g, const ItemF *__restrict__ items, const Chunk *__restrict__ chunks,
+                  const uint32_t *__restrict__ chunk_off, int b0, int nb,
+                  const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
+                  const float *__restrict__ wgt, const PolMat pm, const RowPerm rp,
+                  uint32_t *__restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int T = g.T;
+  const int SW = T + WT - 1, pitch = SW | 1, pstride = SW * pitch;
+  float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][pitch][NP]
+  float *skv = reinterpret_cast<float *>(stage + 2 * NP * pstride);  // [WT][kThreads]: own kv
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float scale_u = 2.f / (float)WT;
+  const float beta = (float)g.beta;
+  const int ntiles = g.ntu * g.ntv;
+  const int64_t plane = (int64_t)g.ngx * g.ngy;
+  const int wk = g.do_w ? WT : 1;
+  const int lo = b0 - (g.S + WT - 2);
+  const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
+  const int s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
+  const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
+  const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
+  __shared__ uint32_t s_ci;
+  for (;;) {
+    if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t ci = s_ci;
+    __syncthreads();  // every thread has read s_ci
+    if (ci >= c_end) break;
+    const Chunk ch = chunks[ci];
+    const int slab = (int)(ch.bucket / (uint32_t)ntiles);
+    const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
+    const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
+    const int kbase = slab * g.S;
+    const int k_lo = max(kbase, b0);
+    const int k_hi = min(min(kbase + g.S + WT - 1, g.nplanes), b0 + nb);
+    const int n = (int)(ch.end - ch.begin);
+    const bool direct = n * WT * WT < SW * SW;
+    const bool has = (int)threadIdx.x < n;
+    ItemF it = items[ch.begin + (has ? threadIdx.x : 0)];
+    const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
+    const int k0 = kbase + (int)((it.loc >> 16) & 0xffu);
+    const int tpar = ((tu + tv) * T) & 1;  // checkerboard parity of the tile origin
+    float ku[WT];
+#pragma unroll
+    for (int a = 0; a < WT; ++a) {
+      const float x = es_kernel(((float)a - it.du) * scale_u, beta);
+      const float y = es_kernel(((float)a - it.dv) * scale_u, beta);
+      ku[a] = ((lu + a + tpar) & 1) ? -x : x;
+      skv[a * kThreads + threadIdx.x] = ((lv + a) & 1) ? -y : y;
+    }
+    // raw sub-grid of plane k -> dst, as one cp.async commit group per thread
+    auto stage_plane = [&](int k, float2 *dst) {
+      const float2 *gp = grid + (int64_t)(k - b0) * NP * plane;
+      for (int r = warp; r < NP * SW; r += kWarps) {
+        const int pol = r / SW, y = r - pol * SW;
+        int q = tv * T + y;
+        while (q >= g.ngy) q -= g.ngy;
+        const float2 *src = gp + pol * plane + (int64_t)rp.row(q) * g.ngx;
+        float2 *d = dst + y * pitch * NP + pol;
+        for (int x = lane; x < SW; x += 32) {
+          int pc = tu * T + x;
+          while (pc >= g.ngx) pc -= g.ngx;
+          cp_async8(d + x * NP, src + pc, true);
+        }
+      }
+      cp_async_commit();
+    };
+    if (!direct && k_lo < k_hi) stage_plane(k_lo, stage);
+    float2 acc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
+    for (int k = k_lo; k < k_hi; ++k) {
+      const float2 *gp = grid + (int64_t)(k - b0) * NP * plane;
+      const float2 *sg = stage + ((k - k_lo) & 1) * NP * pstride;
+      if (!direct) {
+        // plane k + 1 goes to the other buffer (consumed in iteration k - 1,
+        // released by that iteration's closing barrier)
+        if (k + 1 < k_hi) {
+          stage_plane(k + 1, stage + ((k + 1 - k_lo) & 1) * NP * pstride);
+          cp_async_wait1();
+        } else {
+          cp_async_wait0();
+        }
+        __syncthreads();  // plane k staged by every thread
+      }
+      const int aw = k - k0;
+      if (has && aw >= 0 && aw < wk) {
+        const float fw = g.do_w ? es_kernel(((float)aw - it.dwf) * scale_u, beta) : 1.f;
+        float2 sum[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) sum[p] = make_float2(0.f, 0.f);
+#pragma unroll 1
+        for (int b = 0; b < WT; ++b) {
+          float2 rs[NP];
+#pragma unroll
+          for (int p = 0; p < NP; ++p) rs[p] = make_float2(0.f, 0.f);
+          if (direct) {
+            int q = tv * T + lv + b;
+            while (q >= g.ngy) q -= g.ngy;
+            const float2 *row = gp + (int64_t)rp.row(q) * g.ngx;
+#pragma unroll
+            for (int a = 0; a < WT; ++a) {
+              int pc = tu * T + lu + a;
+              while (pc >= g.ngx) pc -= g.ngx;
+#pragma unroll
+              for (int p = 0; p < NP; ++p) {
+                const float2 v = row[p * plane + pc];
+                rs[p].x += ku[a] * v.x;
+                rs[p].y += ku[a] * v.y;
+              }
+            }
+          } else {
+            // a cell's NP values are contiguous: 16-byte loads of two pols
+            const float2 *row = sg + ((lv + b) * pitch + lu) * NP;
+#pragma unroll
+            for (int a = 0; a < WT; ++a) {
+              if constexpr (NP == 1) {
+                const float2 v = row[a];
+                rs[0].x += ku[a] * v.x;
+                rs[0].y += ku[a] * v.y;
+              } else {
+#pragma unroll
+                for (int pp = 0; pp < NP / 2; ++pp) {
+                  const float4 v = *reinterpret_cast<const float4 *>(row + a * NP + 2 * pp);
+                  rs[2 * pp].x += ku[a] * v.x;
+                  rs[2 * pp].y += ku[a] * v.y;
+                  rs[2 * pp + 1].x += ku[a] * v.z;
+                  rs[2 * pp + 1].y += ku[a] * v.w;
+                }
+              }
+            }
+          }
+          const float kvb = skv[b * kThreads + threadIdx.x];
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            sum[p].x += kvb * rs[p].x;
+            sum[p].y += kvb * rs[p].y;
+          }
+        }
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          acc[p].x += fw * sum[p].x;
+          acc[p].y += fw * sum[p].y;
+        }
+      }
+      if (!direct) __syncthreads();  // buffer consumed before it is refilled
+    }
+    if (has && k0 + wk > b0 && k0 < b0 + nb) {
+      float2 v[NP];
+#pragma unroll
+      for (int p = 0; p < NP; ++p) {  // multiply by conj(ph) = exp(+2 pi i w tc)
+        v[p].x = acc[p].x * it.ph.x + acc[p].y * it.ph.y;
+        v[p].y = acc[p].y * it.ph.x - acc[p].x * it.ph.y;
+      }
+      const size_t base = (size_t)it.idx * npv;
+      const bool first = k0 >= b0;
+      for (int q = 0; q < npv; ++q) {
+        float2 o = v[0];
+        if (pm.identity) {
+#pragma unroll
+          for (int p = 1; p < NP; ++p)
+            if (p == (q < NP ? q : NP - 1)) o = v[p];
+        } else {
+          float re = 0.f, im = 0.f;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            const float mr = (float)pm.re[q * pm.nin + p], mi = (float)pm.im[q * pm.nin + p];
+            re += mr * v[p].x - mi * v[p].y;
+            im += mr * v[p].y + mi * v[p].x;
+          }
+          o = make_float2(re, im);
+        }
+        if (wgt) {
+          const float w = wgt[base + q];
+          o.x *= w;
+          o.y *= w;
+        }
+        if (first) {
+          vis[base + q] = o;
+        } else {
+          float2 prev = vis[base + q];
+          prev.x += o.x;
+          prev.y += o.y;
+          vis[base + q] = prev;
+        }
+      }
+    }
+  }
+}
+
+size_t degrid_lane_smem_bytes(const gb_plan *p) {
+  const int SW = p->g.T + p->g.W - 1;
+  return (size_t)2 * p->g.NP * SW * (SW | 1) * sizeof(float2) +
+         (size_t)p->g.W * kThreads * sizeof(float);
+}
+
+// Launch k_degrid_lane<NP, W> for the plan's support (4..16).
+template <int NP>
+static void launch_degrid_lane(const gb_plan *p, unsigned blocks, size_t smem, cudaStream_t s,
+                               const ItemF *items, const Chunk *chunks, const uint32_t *chunk_off,
+                               int b0, int nb, const float2 *grid, float2 *vis, int npv,
+                               const float *wgt, const PolMat &pm, const RowPerm &rp,
+                               uint32_t *counter) {
+#define GB_DL(WV)                                                                            \
+  case WV:                                                                                   \
+    k_degrid_lane<NP, WV><<<blocks, kThreads, smem, s>>>(p->g, items, chunks, chunk_off, b0, \
+                                                         nb, grid, vis, npv, wgt, pm, rp,    \
+                                                         counter);                           \
+    break;
+  switch (p->g.W) {
+    GB_DL(4) GB_DL(5) GB_DL(6) GB_DL(7) GB_DL(8) GB_DL(9) GB_DL(10) GB_DL(11) GB_DL(12)
+    GB_DL(13) GB_DL(14) GB_DL(15) GB_DL(16)
+    default: break;
+  }
+#undef GB_DL
+}
+
+template <int NP>
+static int setup_degrid_lane(gb_plan *p) {
+  const size_t smem = degrid_lane_smem_bytes(p);
+  int per_sm = 0;
+#define GB_DL(WV)                                                                             \
+  case WV:                                                                                    \
+    GB_CUDA(cudaFuncSetAttribute(k_degrid_lane<NP, WV>,                                       \
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));    \
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_degrid_lane<NP, WV>,     \
+                                                          kThreads, smem));                   \
+    break;
+  switch (p->g.W) {
+    GB_DL(4) GB_DL(5) GB_DL(6) GB_DL(7) GB_DL(8) GB_DL(9) GB_DL(10) GB_DL(11) GB_DL(12)
+    GB_DL(13) GB_DL(14) GB_DL(15) GB_DL(16)
+    default:
+      set_error("support %d outside 4..16", p->g.W);
+      return GB_ERR_INVALID_ARG;
+  }
+#undef GB_DL
+  if (per_sm < 1) {
+    set_error("k_degrid_lane cannot launch with %zu bytes of shared memory", smem);
+    return GB_ERR_INVALID_ARG;
+  }
+  p->degrid_blocks = per_sm * p->num_sms;
+  return GB_OK;
+}
+
 template <typename R, int NP>
 static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *wgt,
                          const PolMat &pm, int npv, void *vis, cudaStream_t s) {
@@ -338,6 +595,7 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
                                                            (int64_t)p->num_sms * 32);
   const size_t smem = tile_smem_bytes(p);
   const RowPerm rperm = row_perm(p);
+  C *vis_c = reinterpret_cast<C *>(vis);
   for (int bi = 0; bi < p->nbatches; ++bi) {
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
@@ -357,7 +615,10 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
       GB_LAUNCH_CHECK("k_screen_pad");
     }
     int rc;
-    {
+    if (p->row_fft) {
+      ProfScope ps(kProfRowsFwd, s, 1.5 * gbytes);
+      rc = run_rows(p, grid, b0, nb, -1, s);
+    } else {
       ProfScope ps(kProfFftFwd, s, 2.0 * gbytes);
       rc = run_fft(p, nb, grid, CUFFT_FORWARD, s);
     }
@@ -366,14 +627,20 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
       const double nbi = (double)p->batch_items(b0, nb);
       ProfScope ps(kProfDegrid, s,
                    nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) + gbytes);
-      if (group_lanes(g.W) == 8)
-        k_degrid<R, NP, 8><<<p->degrid_blocks, kThreads, smem, s>>>(
-            g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
-            reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
-      else
-        k_degrid<R, NP, 16><<<p->degrid_blocks, kThreads, smem, s>>>(
-            g, items, chunks, chunk_off, b0, nb, grid, reinterpret_cast<C *>(vis), npv,
-            reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
+      if constexpr (std::is_same<R, float>::value) {
+        launch_degrid_lane<NP>(p, (unsigned)p->degrid_blocks, degrid_lane_smem_bytes(p), s, items,
+                               chunks, chunk_off, b0, nb, grid, vis_c, npv,
+                               reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
+      } else {
+        if (group_lanes(g.W) == 8)
+          k_degrid<R, NP, 8><<<p->degrid_blocks, kThreads, smem, s>>>(
+              g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv,
+              reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
+        else
+          k_degrid<R, NP, 16><<<p->degrid_blocks, kThreads, smem, s>>>(
+              g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv,
+              reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
+      }
       GB_LAUNCH_CHECK("k_degrid");
     }
   }
@@ -416,6 +683,7 @@ static int setup_degrid_aw(gb_plan *p) {
 
 template <typename R, int NP>
 static int setup_degrid_impl(gb_plan *p) {
+  if constexpr (std::is_same<R, float>::value) return setup_degrid_lane<NP>(p);
   return group_lanes(p->g.W) == 8 ? setup_degrid_aw<R, NP, 8>(p)
                                   : setup_degrid_aw<R, NP, 16>(p);
 }

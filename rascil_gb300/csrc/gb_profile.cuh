@@ -28,6 +28,8 @@ enum ProfId {
   kProfColPredA,
   kProfColPredB,
   kProfZeroMargins,
+  kProfRowsInv,
+  kProfRowsFwd,
   kProfCount
 };
 

@@ -135,3 +135,54 @@ def test_modes_agree():
     assert a.device_status() == 0
     a.close()
     b.close()
+
+
+# (nx, ny): grid widths 4096, 8192, 16384 run the library's row kernels
+# (k_rows, one CTA per row, empty rows skipped); short images keep it cheap.
+WIDE = [(2048, 128), (4096, 256), (8192, 128)]
+
+
+@pytest.mark.parametrize("nx,ny", WIDE)
+def test_row_kernel_vs_fp64(nx, ny):
+    c = random_problem(seed=61, nrow=3000, nchan=2, npix=8, pixsize=5e-5, uvscale=30000.0,
+                       wscale=3000.0)
+    pf = _plan(c, nx, ny, True, "fp32", "columns")
+    pd = _plan(c, nx, ny, True, "fp64", "auto", eps=1e-12)
+    assert pf.info["fft_mode"] == 2 and pf.info["own_rows"] == 1
+    vis = c["ms"]
+    d32 = pf.ms2dirty(_dev(vis, torch.complex64)).double().cpu().numpy()
+    d64 = pd.ms2dirty(_dev(vis, torch.complex128)).cpu().numpy()
+    assert rel_rms(d32, d64) < TOL
+    rng = numpy.random.default_rng(8)
+    img = rng.normal(size=(1, nx, ny))
+    v32 = pf.dirty2ms(_dev(img, torch.float32)).cpu().numpy()
+    v64 = pd.dirty2ms(_dev(img, torch.float64)).cpu().numpy()
+    assert rel_rms(v32, v64) < TOL
+    assert pf.device_status() == 0
+    pf.close()
+    pd.close()
+
+
+def test_row_kernel_vs_dft():
+    """Own rows against the direct sum, 4 pols, several plane batches."""
+    nx, ny = 2048, 128
+    c = random_problem(seed=62, nrow=200, nchan=2, npix=8, pixsize=1e-4, uvscale=8000.0,
+                       wscale=2000.0, npol=4)
+    p = _plan(c, nx, ny, True, "fp32", "columns", npol=4,
+              grid_budget_bytes=2 * 4 * 4096 * 256 * 8)
+    assert p.info["own_rows"] == 1 and p.info["planes_per_batch"] < p.info["nplanes"]
+    dirty = p.ms2dirty(_dev(c["ms"], torch.complex64), wgt=_dev(c["wgt"], torch.float32),
+                       layout="xy").double().cpu().numpy()
+    for q in (0, 3):
+        ref = dft.ms2dirty_dft(c["uvw"], c["freq"], c["ms"][..., q], c["wgt"][..., q], nx, ny,
+                               c["pixsize"], c["pixsize"], True)
+        assert rel_rms(dirty[q], ref) < TOL
+    rng = numpy.random.default_rng(9)
+    img = rng.normal(size=(4, nx, ny))
+    vis = p.dirty2ms(_dev(img, torch.float32), layout="xy").cpu().numpy()
+    for q in (1, 2):
+        vref = dft.dirty2ms_dft(c["uvw"], c["freq"], img[q], None, c["pixsize"], c["pixsize"],
+                                True)
+        assert rel_rms(vis[..., q], vref) < TOL
+    assert p.device_status() == 0
+    p.close()
