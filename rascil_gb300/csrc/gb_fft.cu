@@ -222,8 +222,13 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS, 3)
   load_twiddles<N1, 1>(tw, twn, cg.n);
   float2 x[M];
 #pragma unroll
-  for (int m = 0; m < M; ++m)
-    x[m] = ok ? plane[(int64_t)(cg.N2 * (t + T * m) + q2) * cg.ngx + p] : make_float2(0.f, 0.f);
+  for (int m = 0; m < M; ++m) {
+    // rows outside the occupancy mask were never zeroed (nor gridded): load
+    // unconditionally (mask and data loads overlap) and select zero
+    const int row = cg.N2 * (t + T * m) + q2;
+    const float2 v = ok ? plane[(int64_t)row * cg.ngx + p] : make_float2(0.f, 0.f);
+    x[m] = cg.row_used(blockIdx.z, row) ? v : make_float2(0.f, 0.f);
+  }
   __syncthreads();
   float2 y[M / T][T];
   col_dft<N1, 1>(x, xb, tw, t, c, y);
@@ -575,6 +580,11 @@ bool column_split(int n, int &N1, int &N2) {
 
 ColGeom col_geom(const Geom &g) {
   ColGeom cg;
+  cg.mask = nullptr;
+  cg.b0 = 0;
+  cg.NP = g.NP;
+  cg.T = g.T;
+  cg.ntv = g.ntv;
   cg.n = g.ngy;
   column_split(g.ngy, cg.N1, cg.N2);
   cg.ox = (g.ngx - g.nx) / 2;
@@ -684,7 +694,9 @@ template <int NP>
 static int cols_invert_np(gb_plan *p, float2 *grid, int b0, int nb, float *acc, int first,
                           cudaStream_t s) {
   const Geom &g = p->g;
-  const ColGeom cg = col_geom(g);
+  ColGeom cg = col_geom(g);
+  cg.mask = p->at<uint8_t>(p->off_rowmask);
+  cg.b0 = b0;
   const unsigned tiles = (unsigned)((g.nx + kCW - 1) / kCW);
   const float2 *twn = p->at<float2>(p->off_twn);
   const ulonglong2 *screen = g.do_w ? p->at<ulonglong2>(p->off_screen) : nullptr;
@@ -733,7 +745,9 @@ template <int NP>
 static int cols_predict_np(gb_plan *p, const float *img, int b0, int nb, float2 *grid,
                            cudaStream_t s) {
   const Geom &g = p->g;
-  const ColGeom cg = col_geom(g);
+  ColGeom cg = col_geom(g);
+  cg.mask = p->at<uint8_t>(p->off_rowmask);
+  cg.b0 = b0;
   const unsigned tiles = (unsigned)((g.nx + kCW - 1) / kCW);
   const float2 *twn = p->at<float2>(p->off_twn);
   const ulonglong2 *screen = g.do_w ? p->at<ulonglong2>(p->off_screen) : nullptr;
@@ -779,6 +793,29 @@ static int cols_predict_np(gb_plan *p, const float *img, int b0, int nb, float2 
     if (left) GB_CUDA(cudaMemset2DAsync(grid, pitch, 0, left, rows, s));
     if (right) GB_CUDA(cudaMemset2DAsync(grid + cg.ox + g.nx, pitch, 0, right, rows, s));
   }
+  return GB_OK;
+}
+
+// Zero the used rows (mask) of nrows = nb NP ngy rows of ngx cells.
+__global__ void k_zero_rows(float2 *__restrict__ grid, const uint8_t *__restrict__ mask,
+                            int64_t nrows, int ngx, int ngy, int NP, int b0, int T, int ntv) {
+  const int n4 = ngx / 2;  // float4 per row (ngx even)
+  for (int64_t row = blockIdx.x; row < nrows; row += gridDim.x) {
+    const int sp = (int)(row / ngy), r = (int)(row - (int64_t)sp * ngy);
+    if (!mask[(int64_t)(b0 + sp / NP) * ntv + r / T]) continue;
+    float4 *dst = reinterpret_cast<float4 *>(grid + row * ngx);
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) dst[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+int run_zero_rows(gb_plan *p, void *grid, int b0, int nb, cudaStream_t s) {
+  const Geom &g = p->g;
+  const int64_t nrows = (int64_t)nb * g.NP * g.ngy;
+  const unsigned blocks = (unsigned)std::min<int64_t>(nrows, (int64_t)p->num_sms * 8);
+  k_zero_rows<<<blocks, kThreads, 0, s>>>(reinterpret_cast<float2 *>(grid),
+                                          p->at<uint8_t>(p->off_rowmask), nrows, g.ngx, g.ngy,
+                                          g.NP, b0, g.T, g.ntv);
+  GB_LAUNCH_CHECK("k_zero_rows");
   return GB_OK;
 }
 

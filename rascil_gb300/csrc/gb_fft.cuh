@@ -15,6 +15,12 @@ struct ColGeom {
   int nx, ny;      // image size
   int64_t plane;   // ngx * ngy
   int ngx;
+  // (plane, row tile) occupancy: invert step A takes rows outside it as zero
+  const uint8_t *mask;
+  int b0, NP, T, ntv;
+  __device__ __forceinline__ bool row_used(int pp, int q) const {
+    return !mask || mask[(int64_t)(b0 + pp / NP) * ntv + q / T];
+  }
 };
 
 // Row order of a predict grid after the column transforms: logical row
@@ -35,6 +41,9 @@ RowPerm row_perm(const gb_plan *p);
 
 // Shared-memory opt-ins of the column kernels (plan creation).
 int setup_col_kernels(gb_plan *p);
+// Zero the rows of the batch buffer that the occupancy mask marks as used
+// (the others are never read); column mode's replacement for a memset.
+int run_zero_rows(gb_plan *p, void *grid, int b0, int nb, cudaStream_t s);
 // Row lengths with a k_rows instantiation (4096, 8192, 16384).
 bool row_kernel_fits(int n);
 // Occupancy / opt-ins of the row kernels (plan creation).

@@ -167,7 +167,6 @@ __global__ void __launch_bounds__(kThreads)
   const R beta = (R)g.beta;
   const int ntiles = g.ntu * g.ntv;
   const size_t plane = (size_t)g.ngx * g.ngy;
-  const int nrow_steps = (W + LM::RS - 1) / LM::RS;
   int s_lo, s_hi;
   batch_slabs(g, b0, nb, s_lo, s_hi);
   const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
@@ -237,7 +236,9 @@ __global__ void __launch_bounds__(kThreads)
           c[i].y *= f;
         }
         const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
-        for (int r = 0; r < nrow_steps; ++r) {
+        constexpr int kMaxRows = (AW + LM::RS - 1) / LM::RS;  // W <= AW: unrolled, predicated
+#pragma unroll
+        for (int r = 0; r < kMaxRows; ++r) {
           const int b = lm.r0 + r * LM::RS;
           const R kv = __shfl_sync(0xffffffffu, kv_lane, 16 + min(b, W - 1));
           if (b < W && lm.a < W) {
@@ -434,7 +435,14 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
     const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
-    GB_CUDA(cudaMemsetAsync(grid, 0, sizeof(C) * (size_t)nb * NP * plane, s));
+    if (p->col_fft) {  // only rows the gridder writes; column step A skips the rest
+      ProfScope ps(kProfGridZero, s, gbytes);
+      const int rc = run_zero_rows(p, grid, b0, nb, s);
+      if (rc) return rc;
+    } else {
+      ProfScope ps(kProfGridZero, s, gbytes);
+      GB_CUDA(cudaMemsetAsync(grid, 0, sizeof(C) * (size_t)nb * NP * plane, s));
+    }
     {
       ProfScope ps(kProfGrid, s,
                    (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) + gbytes);

@@ -665,7 +665,7 @@ static int layout_workspace(gb_plan *p) {
   p->off_twx = off;
   off = align_up(off + (p->row_fft ? 8 * (size_t)g.ngx : 0));
   p->off_rowmask = off;
-  off = align_up(off + (p->row_fft ? (size_t)g.nplanes * g.ntv : 0));
+  off = align_up(off + (p->col_fft ? (size_t)g.nplanes * g.ntv : 0));
   p->off_tables = off;
   off = align_up(off + 8 * ((size_t)g.nx + g.ny + 2 * kMaxQuad));
   p->off_counters = off;
@@ -785,6 +785,8 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
     k_twiddles<<<(g.ngx + kThreads - 1) / kThreads, kThreads, 0, s>>>(g.ngx,
                                                                      p->at<float2>(p->off_twx));
     GB_LAUNCH_CHECK("k_twiddles");
+  }
+  if (p->col_fft) {
     uint8_t *mask = p->at<uint8_t>(p->off_rowmask);
     GB_CUDA(cudaMemsetAsync(mask, 0, (size_t)g.nplanes * g.ntv, s));
     const unsigned cb = (unsigned)std::min<int64_t>(

@@ -30,6 +30,7 @@ enum ProfId {
   kProfZeroMargins,
   kProfRowsInv,
   kProfRowsFwd,
+  kProfGridZero,
   kProfCount
 };
 
