@@ -435,8 +435,9 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
     const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
+    const double used = p->used_rows(b0, nb);  // profiling byte counts only
     if (p->col_fft) {  // only rows the gridder writes; column step A skips the rest
-      ProfScope ps(kProfGridZero, s, gbytes);
+      ProfScope ps(kProfGridZero, s, used * gbytes);
       const int rc = run_zero_rows(p, grid, b0, nb, s);
       if (rc) return rc;
     } else {
@@ -444,8 +445,10 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
       GB_CUDA(cudaMemsetAsync(grid, 0, sizeof(C) * (size_t)nb * NP * plane, s));
     }
     {
+      // items and their vis read once; the grid rows they reach written once
       ProfScope ps(kProfGrid, s,
-                   (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) + gbytes);
+                   (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) +
+                       used * gbytes);
       if (group_lanes(g.W) == 8)
         k_grid<R, NP, 8><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks,
                                                                 chunk_off, b0, nb, grid,
@@ -458,7 +461,7 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
     }
     int rc;
     if (p->row_fft) {
-      ProfScope ps(kProfRowsInv, s, 1.5 * gbytes);
+      ProfScope ps(kProfRowsInv, s, 1.5 * used * gbytes);  // used rows: read, image half written
       rc = run_rows(p, grid, b0, nb, 1, s);
     } else {
       ProfScope ps(kProfFftInv, s, 2.0 * gbytes);

@@ -793,6 +793,12 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
         ((int64_t)p->max_chunks + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
     k_row_mask<<<cb, kThreads, 0, s>>>(g, chunks, chunk_off, mask);
     GB_LAUNCH_CHECK("k_row_mask");
+    if (prof_on()) {  // host copy for the profiler's byte counts (costs a sync)
+      p->mask_host.assign((size_t)g.nplanes * g.ntv, 0);
+      GB_CUDA(cudaMemcpyAsync(p->mask_host.data(), mask, p->mask_host.size(),
+                              cudaMemcpyDeviceToHost, s));
+      GB_CUDA(cudaStreamSynchronize(s));
+    }
   }
   return GB_OK;
 }

@@ -54,6 +54,17 @@ struct gb_plan {
   int num_sms = 0;
   int grid_blocks = 0, degrid_blocks = 0;  // persistent grid sizes
   std::vector<uint32_t> slab_items;        // host copy: first item of each slab (+ total)
+  std::vector<uint8_t> mask_host;          // host copy of the occupancy mask (profiling)
+
+  // Fraction of the rows of planes [b0, b0 + nb) that visibilities reach
+  // (occupancy mask; 1 without one).  Profiling byte counts only.
+  double used_rows(int b0, int nb) const {
+    if (mask_host.empty() || nb <= 0) return 1.0;
+    int64_t used = 0;
+    for (int k = b0; k < b0 + nb; ++k)
+      for (int t = 0; t < g.ntv; ++t) used += mask_host[(size_t)k * g.ntv + t];
+    return (double)used / ((double)nb * g.ntv);
+  }
 
   // items whose w-slab reaches planes [b0, b0 + nb)
   uint32_t batch_items(int b0, int nb) const {

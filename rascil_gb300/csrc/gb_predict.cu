@@ -616,7 +616,7 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
     }
     int rc;
     if (p->row_fft) {
-      ProfScope ps(kProfRowsFwd, s, 1.5 * gbytes);
+      ProfScope ps(kProfRowsFwd, s, 1.5 * p->used_rows(b0, nb) * gbytes);  // image half in, row out
       rc = run_rows(p, grid, b0, nb, -1, s);
     } else {
       ProfScope ps(kProfFftFwd, s, 2.0 * gbytes);
@@ -625,8 +625,10 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
     if (rc) return rc;
     {
       const double nbi = (double)p->batch_items(b0, nb);
+      // items read, their vis written once; the grid rows they reach read once
       ProfScope ps(kProfDegrid, s,
-                   nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) + gbytes);
+                   nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) +
+                       p->used_rows(b0, nb) * gbytes);
       if constexpr (std::is_same<R, float>::value) {
         launch_degrid_lane<NP>(p, (unsigned)p->degrid_blocks, degrid_lane_smem_bytes(p), s, items,
                                chunks, chunk_off, b0, nb, grid, vis_c, npv,

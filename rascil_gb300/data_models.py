@@ -18,6 +18,8 @@ imaging functions accept either these or RASCIL's own objects.
 """
 
 import copy
+import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy
 
@@ -56,6 +58,29 @@ class SkyDirection:
 
     def __repr__(self):
         return "SkyDirection(ra=%.9f rad, dec=%.9f rad)" % (self.ra.rad, self.dec.rad)
+
+
+_PARALLEL_MIN_BYTES = 64 << 20
+
+
+def parallel_copy(a):
+    """Copy of a numpy array; large C-contiguous arrays are copied in
+    os.cpu_count() slices on threads (numpy.copyto releases the GIL), which
+    matters for the multi-GB visibility, flag and weight arrays."""
+    a = numpy.asarray(a)
+    if a.nbytes < _PARALLEL_MIN_BYTES or not a.flags.c_contiguous:
+        return a.copy()
+    out = numpy.empty_like(a)
+    src, dst = a.reshape(-1), out.reshape(-1)
+    nthreads = max(1, min(32, os.cpu_count() or 1))
+    step = -(-src.size // nthreads)
+
+    def part(i):
+        numpy.copyto(dst[i * step:(i + 1) * step], src[i * step:(i + 1) * step])
+
+    with ThreadPoolExecutor(nthreads) as ex:
+        list(ex.map(part, range(nthreads)))
+    return out
 
 
 class DataArray:
@@ -151,8 +176,17 @@ class Image:
     def image_acc(self):
         return _ImageAccessor(self)
 
-    def copy(self, deep=True):
-        return copy.deepcopy(self) if deep else copy.copy(self)
+    def copy(self, deep=True, pixels=None):
+        """Copy; ``deep`` copies the pixels (in parallel), ``pixels`` gives
+        the copy a new pixel array instead."""
+        if not deep and pixels is None:
+            return copy.copy(self)
+        new = copy.copy(self)
+        new._wcs = copy.deepcopy(self._wcs)
+        new.attrs = copy.deepcopy(self.attrs)
+        data = self._vars["pixels"].data
+        new._vars = {"pixels": DataArray(parallel_copy(data) if pixels is None else pixels)}
+        return new
 
 
 def create_image(npixel, cellsize, phasecentre, frequency=(1e8,), channel_bandwidth=(1e6,),
@@ -250,9 +284,27 @@ class BlockVisibility:
         return _BVisAccessor(self)
 
 
-def copy_visibility(bvis, zero=False):
-    """Deep copy, optionally zeroing vis (``visibility/base.py:105-118``)."""
-    new = copy.deepcopy(bvis)
-    if zero:
-        new["vis"].data[...] = 0.0
+def copy_visibility(bvis, zero=False, vis=None):
+    """Deep copy, optionally zeroing vis (``visibility/base.py:105-118``).
+    The arrays are copied in parallel; ``vis`` (same shape) becomes the
+    copy's visibilities instead of a copy or zeros (predict writes the whole
+    array, so copying or zeroing it first would be wasted)."""
+    if not isinstance(bvis, BlockVisibility):
+        new = copy.deepcopy(bvis)
+        if vis is not None:
+            new["vis"].data = vis
+        elif zero:
+            new["vis"].data[...] = 0.0
+        return new
+    new = copy.copy(bvis)
+    new.__dict__ = {k: copy.deepcopy(v) for k, v in bvis.__dict__.items() if k != "_vars"}
+    new._vars = {}
+    for key, arr in bvis._vars.items():
+        if key == "vis" and vis is not None:
+            assert vis.shape == arr.data.shape
+            new._vars[key] = DataArray(vis)
+        elif key == "vis" and zero:
+            new._vars[key] = DataArray(numpy.zeros_like(arr.data))
+        else:
+            new._vars[key] = DataArray(parallel_copy(arr.data))
     return new

@@ -13,7 +13,10 @@ Same signatures, keyword arguments, defaults and results as
   ``.T`` of ``ng.py:94,249`` costs nothing;
 * MFS (``ng.py:227-250``): one plan over all channels.  Per-channel
   (``ng.py:251-277``): one plan per image channel over the visibility
-  channels that map to it (their sum is what ng.py accumulates).
+  channels that map to it (their sum is what ng.py accumulates);
+* images accumulate and are normalised by sumwt on the device; host
+  arrays in page-locked memory move by direct DMA, and results come back
+  into page-locked arrays (torch's host caching allocator).
 
 Extra keyword arguments: ``precision`` ("fp64", the default, matches
 the reference's complex128 path; "fp32" is the fast form), ``device``.
@@ -28,7 +31,7 @@ import torch
 from ..data_models import copy_visibility
 from ..polarisation import conversion_matrix
 from ..wgridder import Plan
-from .base import image_is_canonical, normalise_sumwt, shift_vis_to_image
+from .base import image_is_canonical, shift_vis_to_image
 
 log = logging.getLogger("rascil-logger")
 
@@ -48,8 +51,8 @@ def _vis_to_im(model, freq):
 
 
 def _device_uvw(uvw, device, nan_to_num=False):
-    u = torch.from_numpy(numpy.ascontiguousarray(uvw.reshape(-1, 3), dtype=numpy.float64))
-    u = u.to(device)
+    u = _to_device(numpy.ascontiguousarray(uvw.reshape(-1, 3), dtype=numpy.float64), None,
+                   device)
     if nan_to_num:
         u = torch.nan_to_num(u)
     u[:, 0].neg_()
@@ -58,7 +61,23 @@ def _device_uvw(uvw, device, nan_to_num=False):
 
 
 def _to_device(x, dtype, device):
-    return torch.from_numpy(numpy.ascontiguousarray(x)).to(device=device).to(dtype)
+    """Host array -> device tensor.  From page-locked memory the copy is a
+    direct DMA; a dtype conversion (dtype not None) happens on the device."""
+    t = torch.from_numpy(numpy.ascontiguousarray(x))
+    t = t.to(device=device, non_blocking=t.is_pinned())
+    return t if dtype is None else t.to(dtype)
+
+
+def _torch_dtype(np_dtype):
+    return torch.from_numpy(numpy.zeros(0, dtype=np_dtype)).dtype
+
+
+def _to_host(t, dtype):
+    """Device tensor -> numpy array in page-locked memory (torch's host
+    caching allocator), so the copy is a direct DMA."""
+    host = torch.empty(t.shape, dtype=dtype, pin_memory=t.is_cuda)
+    host.copy_(t)
+    return host.numpy()
 
 
 def predict_ng(bvis, model, **kwargs):
@@ -73,7 +92,6 @@ def predict_ng(bvis, model, **kwargs):
     cdt = torch.complex128 if precision == "fp64" else torch.complex64
     rdt = torch.float64 if precision == "fp64" else torch.float32
 
-    newbvis = copy_visibility(bvis, zero=True)
     freq = numpy.asarray(bvis.frequency.data, dtype=numpy.float64)
     nrows, nbaselines, vnchan, vnpol = bvis.vis.shape
     m_nchan, m_npol, ny, nx = model["pixels"].data.shape
@@ -83,7 +101,7 @@ def predict_ng(bvis, model, **kwargs):
     polmat = conversion_matrix(model.image_acc.polarisation_frame,
                                bvis.blockvisibility_acc.polarisation_frame)
     pm = None if numpy.array_equal(polmat, numpy.eye(vnpol)) else polmat
-    uvw = _device_uvw(newbvis.uvw.data, device, nan_to_num=True)
+    uvw = _device_uvw(bvis.uvw.data, device, nan_to_num=True)
     pixels = model["pixels"].data
     out = torch.empty((nrows * nbaselines, vnchan, vnpol), dtype=cdt, device=device)
     if m_nchan == 1:
@@ -103,17 +121,25 @@ def predict_ng(bvis, model, **kwargs):
             out = vis
         else:
             out[:, torch.from_numpy(chans).to(device), :] = vis
-    result = out.reshape(nrows, nbaselines, vnchan, vnpol).cpu().numpy()
-    if newbvis["vis"].data.dtype != result.dtype:
-        result = result.astype(newbvis["vis"].data.dtype)
-    newbvis["vis"].data = result
+    vdt = bvis["vis"].data.dtype
+    out = out.reshape(nrows, nbaselines, vnchan, vnpol)
+    if vdt == numpy.complex128 and out.dtype != torch.complex128:
+        out = out.to(torch.complex128)
+    elif vdt == numpy.complex64 and out.dtype != torch.complex64:
+        out = out.to(torch.complex64)
+    result = _to_host(out, out.dtype)
+    if result.dtype != vdt:
+        result = result.astype(vdt)
+    # ng.py:56 deep-copies the input and zeroes vis; the copy gets the
+    # predicted visibilities directly instead
+    newbvis = copy_visibility(bvis, vis=result)
     return shift_vis_to_image(newbvis, model, tangent=True, inverse=True)
 
 
 def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
     """Invert visibilities to (image, sumwt) (``ng.py:136-282``)."""
     assert image_is_canonical(model)
-    im = model.copy(deep=True)
+    im = model
     epsilon = get_parameter(kwargs, "epsilon", 1e-12)
     do_wstacking = get_parameter(kwargs, "do_wstacking", True)
     precision = get_parameter(kwargs, "precision", "fp64")
@@ -135,13 +161,13 @@ def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
     vis = None
     if not dopsf:
         vis = _to_device(sbvis["vis"].data.reshape(R, vnchan, vnpol), cdt, device)
-    flags = torch.from_numpy(numpy.ascontiguousarray(
-        sbvis["flags"].data.reshape(R, vnchan, vnpol))).to(device)
+    flags = _to_device(sbvis["flags"].data.reshape(R, vnchan, vnpol), None, device)
     if flags.dtype != torch.int64:
         flags = (flags != 0).to(torch.uint8)
     wgt = _to_device(sbvis["imaging_weight"].data.reshape(R, vnchan, vnpol), rdt, device)
 
-    im["pixels"].data[...] = 0.0
+    pdt = model["pixels"].data.dtype
+    acc = torch.zeros((nchan, npol, ny, nx), dtype=torch.float64, device=device)
     sumwt = numpy.zeros([nchan, npol])
     mfs = nchan == 1 and vnchan > 1
     if mfs:
@@ -161,14 +187,17 @@ def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
         try:
             dirty, sw = plan.ms2dirty(pick(vis), wgt=pick(wgt), flags=pick(flags), polmat=pm,
                                       psf=dopsf, layout="yx", sumwt=True)
-            dirty = dirty.cpu().numpy()
+            acc[ichan] += dirty
             sw = sw.cpu().numpy()
         finally:
             plan.close()
-        im["pixels"].data[ichan] += dirty
         sumwt[ichan] += sw
-    if normalise:
-        im = normalise_sumwt(im, sumwt)
+    if normalise:  # normalise_sumwt (imaging/base.py:109-162), on the device
+        scale = numpy.where(sumwt > 0.0, 1.0 / numpy.where(sumwt > 0.0, sumwt, 1.0), 0.0)
+        acc *= torch.from_numpy(scale).to(device)[:, :, None, None]
+    # the new image: the model's metadata (deep-copied) with the dirty pixels
+    pdt = _torch_dtype(pdt)
+    im = model.copy(deep=True, pixels=_to_host(acc if acc.dtype == pdt else acc.to(pdt), pdt))
     return im, sumwt
 
 
