@@ -62,4 +62,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
   return false;
 }
 
+// Bulk prefetch of [p, p + bytes) into L2 (TMA unit, no shared memory);
+// p 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
+
 }  // namespace gb

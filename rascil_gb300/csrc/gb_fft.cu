@@ -500,15 +500,30 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
   }
   __syncthreads();
   auto tw = [&](int m) { return cmul(ta[m >> 7], tb[m & 127]); };
-  const int t = threadIdx.x;
-  for (int64_t row = blockIdx.x; row < ra.nrows; row += gridDim.x) {
-    if (ra.mask) {
-      const int sp = (int)(row / ra.ngy), r = (int)(row - (int64_t)sp * ra.ngy);
-      const int q = ra.perm_s1 < 0 ? r
-                                   : (r >> ra.perm_s2) + ((r & ((1 << ra.perm_s2) - 1)) << ra.perm_s1);
-      const int k = ra.b0 + sp / ra.NP;
-      if (!ra.mask[(int64_t)k * ra.ntv + q / ra.T]) continue;  // uniform over the CTA
+  auto used = [&](int64_t row) {
+    if (!ra.mask) return true;
+    const int sp = (int)(row / ra.ngy), r = (int)(row - (int64_t)sp * ra.ngy);
+    const int q = ra.perm_s1 < 0 ? r
+                                 : (r >> ra.perm_s2) + ((r & ((1 << ra.perm_s2) - 1)) << ra.perm_s1);
+    return ra.mask[(int64_t)(ra.b0 + sp / ra.NP) * ra.ntv + q / ra.T] != 0;
+  };
+  // the next used row this CTA will transform, prefetched into L2 while
+  // this one is transformed (one CTA per SM leaves no other row in flight)
+  auto next_used = [&](int64_t row) {
+    for (row += gridDim.x; row < ra.nrows && !used(row); row += gridDim.x) {
     }
+    return row;
+  };
+  auto prefetch_row = [&](int64_t row) {
+    if (threadIdx.x == 0 && row < ra.nrows)
+      prefetch_l2(ra.grid + row * N + ra.in_lo, (unsigned)((ra.in_hi - ra.in_lo) * sizeof(float2)));
+  };
+  const int t = threadIdx.x;
+  int64_t row = blockIdx.x;
+  if (row < ra.nrows && !used(row)) row = next_used(row);
+  prefetch_row(row);
+  for (; row < ra.nrows; row = next_used(row)) {
+    prefetch_row(next_used(row));
     float2 *rp = ra.grid + row * N;
     // pass 1
     float2 x[R1];

@@ -160,6 +160,13 @@ __global__ void __launch_bounds__(kThreads)
   A *acc = reinterpret_cast<A *>(smem_raw);  // [re pols | im pols][SW][pitch]
   const int W = g.W, T = g.T;
   const TileLayout L = tile_layout(T, W, NP);
+  // FP32: per-chunk cache of every item's kernel values {loc, ku[W], kv[W],
+  // kw[W]} and scaled gridded values, computed once per chunk instead of
+  // once per item and plane
+  constexpr bool kCache = std::is_same<R, float>::value;
+  const int KS = 3 * W + 1;
+  R *kc = reinterpret_cast<R *>(acc + 2 * NP * L.plane);     // [kChunkItems][KS]
+  C *cc = reinterpret_cast<C *>(kc + kChunkItems * KS);      // [kChunkItems][NP]
   const int SW = L.SW, SW2 = SW * SW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const LM lm(lane);
@@ -212,30 +219,70 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
     __syncthreads();  // s_red and s_ci are reused by the next chunk
+    if constexpr (kCache) {
+      const R f = direct ? (R)1 : scale;
+      for (int jj = threadIdx.x; jj < n; jj += kThreads) {
+        const auto it = items[ch.begin + jj];
+        R *c = kc + jj * KS;
+        c[0] = __uint_as_float(it.loc);
+        for (int a = 0; a < W; ++a) {
+          c[1 + a] = es_kernel(((R)a - it.du) * scale_u, beta);
+          c[1 + W + a] = es_kernel(((R)a - it.dv) * scale_u, beta);
+          c[1 + 2 * W + a] = g.do_w ? es_kernel(((R)a - it.dwf) * scale_u, beta) : (R)1;
+        }
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          C v = cvis[(size_t)(ch.begin + jj) * NP + p];
+          v.x *= f;
+          v.y *= f;
+          cc[jj * NP + p] = v;
+        }
+      }
+      __syncthreads();
+    }
     for (int k = k_lo; k < k_hi; ++k) {
       C *gplane = grid + (size_t)(k - b0) * NP * plane;
       for (uint32_t j = ch.begin + warp; j < ch.end; j += kWarps) {
-        const auto it = items[j];
-        const int aw = k - (kbase + (int)((it.loc >> 16) & 0xffu));
-        if (aw < 0 || aw >= W) continue;
-        const R fw = g.do_w ? es_kernel(((R)aw - it.dwf) * scale_u, beta) : (R)1;
-        // lanes 0..15 hold the u kernel values, 16..31 the v values
-        R kv_lane = (R)0;
-        if (lane < 16) {
-          if (lane < W) kv_lane = es_kernel(((R)lane - it.du) * scale_u, beta);
-        } else if (lane - 16 < W) {
-          kv_lane = es_kernel(((R)(lane - 16) - it.dv) * scale_u, beta);
-        }
-        const R ku = __shfl_sync(0xffffffffu, kv_lane, lm.a);
+        const int jj = (int)(j - ch.begin);
+        R fw, ku, kv_lane = (R)0;
+        uint32_t loc;
         C c[LM::NPL];
+        if constexpr (kCache) {
+          const R *kj = kc + jj * KS;
+          loc = __float_as_uint(kj[0]);
+          const int aw = k - (kbase + (int)((loc >> 16) & 0xffu));
+          if (aw < 0 || aw >= W) continue;
+          fw = kj[1 + 2 * W + aw];
+          ku = lm.a < W ? kj[1 + lm.a] : (R)0;
+          if (lane >= 16 && lane - 16 < W) kv_lane = kj[1 + W + lane - 16];
 #pragma unroll
-        for (int i = 0; i < LM::NPL; ++i) {
-          c[i] = cvis[(size_t)j * NP + lm.pol(i)];
-          const R f = fw * (direct ? (R)1 : scale);
-          c[i].x *= f;
-          c[i].y *= f;
+          for (int i = 0; i < LM::NPL; ++i) {
+            c[i] = cc[jj * NP + lm.pol(i)];
+            c[i].x *= fw;
+            c[i].y *= fw;
+          }
+        } else {
+          const auto it = items[j];
+          loc = it.loc;
+          const int aw = k - (kbase + (int)((it.loc >> 16) & 0xffu));
+          if (aw < 0 || aw >= W) continue;
+          fw = g.do_w ? es_kernel(((R)aw - it.dwf) * scale_u, beta) : (R)1;
+          // lanes 0..15 hold the u kernel values, 16..31 the v values
+          if (lane < 16) {
+            if (lane < W) kv_lane = es_kernel(((R)lane - it.du) * scale_u, beta);
+          } else if (lane - 16 < W) {
+            kv_lane = es_kernel(((R)(lane - 16) - it.dv) * scale_u, beta);
+          }
+          ku = __shfl_sync(0xffffffffu, kv_lane, lm.a);
+#pragma unroll
+          for (int i = 0; i < LM::NPL; ++i) {
+            c[i] = cvis[(size_t)j * NP + lm.pol(i)];
+            const R f = fw * (direct ? (R)1 : scale);
+            c[i].x *= f;
+            c[i].y *= f;
+          }
         }
-        const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
+        const int lu = (int)(loc & 0xffu), lv = (int)((loc >> 8) & 0xffu);
         constexpr int kMaxRows = (AW + LM::RS - 1) / LM::RS;  // W <= AW: unrolled, predicated
 #pragma unroll
         for (int r = 0; r < kMaxRows; ++r) {
@@ -396,6 +443,14 @@ size_t tile_smem_bytes(const gb_plan *p) {
   return (size_t)2 * p->g.NP * L.plane * real_bytes(p->precision);
 }
 
+// k_grid: the sub-grid plus, in the FP32 form, the per-chunk item cache.
+size_t grid_smem_bytes(const gb_plan *p) {
+  size_t b = tile_smem_bytes(p);
+  if (p->precision == GB_FP32)
+    b += (size_t)kChunkItems * ((3 * p->g.W + 1) * sizeof(float) + p->g.NP * sizeof(float2));
+  return b;
+}
+
 template <typename R, int NP>
 static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
                          const void *flags, int ftype, const PolMat &pm, int psf, void *dirty,
@@ -430,7 +485,7 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
   const int64_t npix = (int64_t)g.nx * g.ny;
   const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
                                                           (int64_t)p->num_sms * 32);
-  const size_t smem = tile_smem_bytes(p);
+  const size_t smem = grid_smem_bytes(p);
   for (int bi = 0; bi < p->nbatches; ++bi) {
     const int b0 = bi * g.B;
     const int nb = std::min(g.B, g.nplanes - b0);
@@ -516,7 +571,7 @@ int run_ms2dirty(gb_plan *p, const void *vis, int npv, const void *wgt, const vo
 
 template <typename R, int NP, int AW>
 static int setup_grid_aw(gb_plan *p) {
-  const size_t smem = tile_smem_bytes(p);
+  const size_t smem = grid_smem_bytes(p);
   GB_CUDA(cudaFuncSetAttribute(k_grid<R, NP, AW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
   int per_sm = 0;
