@@ -494,9 +494,14 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
   float2 *ex = smem;                        // exchange: max(R1 (TN + 1), N) cells
   float2 *ta = smem + R1 * (TN + 1);        // [NA]
   float2 *tb = ta + NA;                     // [128]
+  float2 *t2 = tb + 128;                    // [TN]: w_TN^m = w_N^(R1 m)
   for (int i = threadIdx.x; i < NA + 128; i += TH) {
     const float2 w = ra.twx[i < NA ? i * 128 : i - NA];
     (i < NA ? ta[i] : tb[i - NA]) = S > 0 ? w : conjf2(w);
+  }
+  for (int i = threadIdx.x; i < TN; i += TH) {
+    const float2 w = ra.twx[i * R1];
+    t2[i] = S > 0 ? w : conjf2(w);
   }
   __syncthreads();
   auto tw = [&](int m) { return cmul(ta[m >> 7], tb[m & 127]); };
@@ -533,8 +538,26 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
       x[m] = (col >= ra.in_lo && col < ra.in_hi) ? rp[col] : make_float2(0.f, 0.f);
     }
     dft<R1, S>(x);
+    {
+      // w^(t k1), k1 < 32, as w^(t (k1 & 7)) w^(8 t (k1 >> 3)): powers of w^t
+      // by multiplication (at most 7 roundings) times three table values
+      float2 pw[8], qw[4];
+      pw[0] = make_float2(1.f, 0.f);
+      pw[1] = tw(t);
 #pragma unroll
-    for (int k1 = 0; k1 < R1; ++k1) ex[k1 * (TN + 1) + t] = k1 ? cmul(x[k1], tw(t * k1)) : x[k1];
+      for (int j = 2; j < 8; ++j) pw[j] = cmul(pw[j - 1], pw[1]);
+      qw[0] = pw[0];
+#pragma unroll
+      for (int i = 1; i < R1 / 8; ++i) qw[i] = tw((8 * t * i) & (N - 1));
+      static_assert(R1 == 32, "pass-1 twiddle split");
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) {
+        float2 v = x[k1];
+        if (k1 & 7) v = cmul(v, pw[k1 & 7]);
+        if (k1 >> 3) v = cmul(v, qw[k1 >> 3]);
+        ex[k1 * (TN + 1) + t] = v;
+      }
+    }
     __syncthreads();
     // pass 2: units u = k1 + R1 s
     constexpr int U2 = R1 * R3 / TH;
@@ -546,7 +569,7 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
       for (int m = 0; m < R2; ++m) y[i][m] = ex[k1 * (TN + 1) + s + R3 * m];
       dft<R2, S>(y[i]);
 #pragma unroll
-      for (int k = 1; k < R2; ++k) y[i][k] = cmul(y[i][k], tw(s * k * R1));
+      for (int k = 1; k < R2; ++k) y[i][k] = cmul(y[i][k], t2[s * k]);
     }
     __syncthreads();
 #pragma unroll
@@ -838,7 +861,8 @@ bool row_kernel_fits(int n) { return n == 4096 || n == 8192 || n == 16384; }
 
 template <int N> constexpr size_t rows_smem() {
   using RS = RowShape<N>;
-  return sizeof(float2) * ((size_t)RS::R1 * (RS::R2 * RS::R3 + 1) + N / 128 + 128);
+  return sizeof(float2) *
+         ((size_t)RS::R1 * (RS::R2 * RS::R3 + 1) + N / 128 + 128 + RS::R2 * RS::R3);
 }
 
 template <int N, int S> static int rows_occupancy(int *per_sm) {
