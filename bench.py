@@ -375,6 +375,7 @@ def e2e_run(wl, steps):
     import torch
     from rascil_gb300 import simulation as sim
     from rascil_gb300.imaging import invert_ng, predict_ng
+    from rascil_gb300.imaging.ng import clear_plan_cache
     from rascil_gb300.data_models import BlockVisibility
     from rascil_gb300.polarisation import PolarisationFrame
 
@@ -398,6 +399,9 @@ def e2e_run(wl, steps):
     kw = dict(epsilon=wl.epsilon, precision="fp32", do_wstacking=True)
 
     def one():
+        # one plan per step, as in the device-timed steps: invert builds it,
+        # predict reuses it through the API's plan cache
+        clear_plan_cache()
         im, sw = invert_ng(bvis, model, **kw)
         pv = predict_ng(bvis, model, **kw)
         return im, pv

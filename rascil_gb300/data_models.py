@@ -299,6 +299,7 @@ def copy_visibility(bvis, zero=False, vis=None):
     new = copy.copy(bvis)
     new.__dict__ = {k: copy.deepcopy(v) for k, v in bvis.__dict__.items() if k != "_vars"}
     new._vars = {}
+    copied = {}  # arrays shared inside the input stay shared in the copy (as deepcopy)
     for key, arr in bvis._vars.items():
         if key == "vis" and vis is not None:
             assert vis.shape == arr.data.shape
@@ -306,5 +307,7 @@ def copy_visibility(bvis, zero=False, vis=None):
         elif key == "vis" and zero:
             new._vars[key] = DataArray(numpy.zeros_like(arr.data))
         else:
-            new._vars[key] = DataArray(parallel_copy(arr.data))
+            if id(arr.data) not in copied:
+                copied[id(arr.data)] = parallel_copy(arr.data)
+            new._vars[key] = DataArray(copied[id(arr.data)])
     return new

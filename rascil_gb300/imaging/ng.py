@@ -24,6 +24,8 @@ the reference's complex128 path; "fp32" is the fast form), ``device``.
 """
 
 import logging
+import os
+import threading
 
 import numpy
 import torch
@@ -35,7 +37,7 @@ from .base import image_is_canonical, shift_vis_to_image
 
 log = logging.getLogger("rascil-logger")
 
-__all__ = ["predict_ng", "invert_ng", "predict_gb", "invert_gb"]
+__all__ = ["predict_ng", "invert_ng", "predict_gb", "invert_gb", "clear_plan_cache"]
 
 
 def get_parameter(kwargs, key, default=None):
@@ -80,6 +82,89 @@ def _to_host(t, dtype):
     return host.numpy()
 
 
+# One-entry plan cache: RASCIL pipelines call invert_ng and predict_ng on the
+# same visibilities, so the second call can reuse the first one's plan (its
+# bucket sort and tables) instead of building it again.  A cached plan is
+# reused only when the geometry and parameters match and the uvw just
+# uploaded are equal, element for element on the device, to the plan's own.
+# A plan in use is checked out of the cache, so concurrent callers never
+# share one.  RASCIL_GB300_PLAN_CACHE=0 disables it.
+_plan_cache = {}
+_spare_ws = []  # at most one device workspace of a closed plan, reused by the next
+_plan_lock = threading.Lock()
+
+
+def _cache_on():
+    return os.environ.get("RASCIL_GB300_PLAN_CACHE", "1") != "0"
+
+
+def _retire(plan):
+    """Close a plan and keep its workspace for the next plan (a multi-GB
+    buffer; allocating it anew each call costs more than the transfers)."""
+    ws = plan.workspace
+    plan.close()
+    if ws is None:
+        return
+    with _plan_lock:
+        keep = [w for w in _spare_ws + [ws] if w.device == ws.device]
+        keep.sort(key=lambda w: w.numel())
+        _spare_ws[:] = keep[-1:]
+
+
+def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision):
+    plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=npol,
+                precision=precision, bind=False)
+    need = max(plan.workspace_bytes, 256)
+    ws = None
+    with _plan_lock:
+        for i, w in enumerate(_spare_ws):
+            if w.device == uvw.device and w.numel() >= need:
+                ws = _spare_ws.pop(i)
+                break
+    if ws is None:
+        ws = torch.empty(need, dtype=torch.uint8, device=uvw.device)
+    plan.bind(ws)
+    return plan
+
+
+def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision):
+    key = (uvw.device, tuple(uvw.shape), tuple(f.cpu().tolist()), nx, ny, float(pixsize),
+           float(epsilon), bool(do_wstacking), int(npol), precision)
+    if _cache_on():
+        with _plan_lock:
+            hit = _plan_cache.pop(key, None)
+        if hit is not None:
+            if torch.equal(hit[0], uvw):
+                return key, hit
+            _retire(hit[1])
+    return key, (uvw, _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision))
+
+
+def _checkin_plan(key, entry):
+    if not _cache_on():
+        _retire(entry[1])
+        return
+    with _plan_lock:
+        old = list(_plan_cache.values())
+        _plan_cache.clear()
+        _plan_cache[key] = entry
+    for _, plan in old:
+        _retire(plan)
+
+
+def clear_plan_cache(release_memory=False):
+    """Drop the cached plan, so the next call sorts its visibilities again.
+    Its device workspace is kept for the next plan unless release_memory."""
+    with _plan_lock:
+        old = list(_plan_cache.values())
+        _plan_cache.clear()
+    for _, plan in old:
+        _retire(plan)
+    if release_memory:
+        with _plan_lock:
+            _spare_ws.clear()
+
+
 def predict_ng(bvis, model, **kwargs):
     """Predict visibilities from a model image (``ng.py:33-133``)."""
     assert image_is_canonical(model)
@@ -110,13 +195,13 @@ def predict_ng(bvis, model, **kwargs):
         groups = [(ic, numpy.nonzero(vis_to_im == ic)[0]) for ic in numpy.unique(vis_to_im)]
     for ichan, chans in groups:
         f = torch.from_numpy(numpy.ascontiguousarray(freq[chans])).to(device)
-        plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=m_npol,
-                    precision=precision)
+        key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, m_npol,
+                                    precision)
         try:
             img = _to_device(pixels[ichan], rdt, device)
-            vis = plan.dirty2ms(img, polmat=pm, npol_vis=vnpol, layout="yx")
+            vis = entry[1].dirty2ms(img, polmat=pm, npol_vis=vnpol, layout="yx")
         finally:
-            plan.close()
+            _checkin_plan(key, entry)
         if len(chans) == vnchan:
             out = vis
         else:
@@ -182,15 +267,15 @@ def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
         def pick(t):
             return t if (t is None or whole) else t[:, sel, :].contiguous()
 
-        plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=npol,
-                    precision=precision)
+        key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol,
+                                    precision)
         try:
-            dirty, sw = plan.ms2dirty(pick(vis), wgt=pick(wgt), flags=pick(flags), polmat=pm,
-                                      psf=dopsf, layout="yx", sumwt=True)
+            dirty, sw = entry[1].ms2dirty(pick(vis), wgt=pick(wgt), flags=pick(flags),
+                                          polmat=pm, psf=dopsf, layout="yx", sumwt=True)
             acc[ichan] += dirty
             sw = sw.cpu().numpy()
         finally:
-            plan.close()
+            _checkin_plan(key, entry)
         sumwt[ichan] += sw
     if normalise:  # normalise_sumwt (imaging/base.py:109-162), on the device
         scale = numpy.where(sumwt > 0.0, 1.0 / numpy.where(sumwt > 0.0, sumwt, 1.0), 0.0)

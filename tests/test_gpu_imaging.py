@@ -169,3 +169,35 @@ def test_gpu_component_dft_matches_oracle():
     fast = dft_components(torch.from_numpy(uvw).cuda(), torch.from_numpy(freq).cuda(), lmn,
                           flux, precision="fp32", exact=False).cpu().numpy()
     assert rel_rms(fast, ref) < 1e-6
+
+
+def test_plan_cache_reuse_and_invalidation(monkeypatch):
+    """invert_ng then predict_ng on the same visibilities reuse one plan; the
+    results equal those without the cache, and uvw changed in place between
+    the calls are noticed (the cached plan is rebuilt, not reused)."""
+    from rascil_gb300.imaging import invert_ng, predict_ng
+    from rascil_gb300.imaging import ng
+    uvw, freq, pc, cfg, src, bvis, model, u, f = _c1_data("fp32", ntimes=16)
+    kw = dict(epsilon=1e-5, precision="fp32")
+    ng.clear_plan_cache()
+    monkeypatch.setenv("RASCIL_GB300_PLAN_CACHE", "1")
+    im_c, sw_c = invert_ng(bvis, model, **kw)
+    assert len(ng._plan_cache) == 1
+    v_c = predict_ng(bvis, model, **kw)["vis"].data
+    monkeypatch.setenv("RASCIL_GB300_PLAN_CACHE", "0")
+    im_n, sw_n = invert_ng(bvis, model, **kw)
+    v_n = predict_ng(bvis, model, **kw)["vis"].data
+    numpy.testing.assert_array_equal(sw_c, sw_n)
+    assert rel_rms(im_c["pixels"].data, im_n["pixels"].data) < 1e-6
+    numpy.testing.assert_array_equal(v_c, v_n)  # one thread per item: deterministic sums
+    # uvw scaled in place after the cached invert: predict must see the new uvw
+    monkeypatch.setenv("RASCIL_GB300_PLAN_CACHE", "1")
+    ng.clear_plan_cache()
+    invert_ng(bvis, model, **kw)
+    bvis.uvw.data[...] *= 1.01
+    v_c2 = predict_ng(bvis, model, **kw)["vis"].data
+    monkeypatch.setenv("RASCIL_GB300_PLAN_CACHE", "0")
+    v_n2 = predict_ng(bvis, model, **kw)["vis"].data
+    numpy.testing.assert_array_equal(v_c2, v_n2)
+    assert rel_rms(v_c2, v_n) > 1e-3
+    ng.clear_plan_cache(release_memory=True)
