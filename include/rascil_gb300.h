@@ -46,7 +46,8 @@ typedef enum {
   GB_ERR_CUDA = 4,
   GB_ERR_CUFFT = 5,
   GB_ERR_TIMEOUT = 6,
-  GB_ERR_INTERNAL = 7
+  GB_ERR_INTERNAL = 7,
+  GB_ERR_OUT_OF_GRID = 8
 } gb_status;
 
 typedef enum { GB_FP32 = 0, GB_FP64 = 1 } gb_precision;
@@ -261,6 +262,36 @@ int gb_profile_get(int32_t index, char *name, int32_t name_len, double *total_ms
  * that overlap on the GPU race. */
 int gb_wrange_noalloc(const double *uvw_dev, const double *freq_dev, int64_t nrows,
                       int32_t nchan, double *out_dev, void *stream);
+
+/* Imaging weights: RASCIL's weight_visibility
+ * (rascil/processing_components/imaging/weighting.py:27-48, with
+ * grid_blockvisibility_weight_to_griddata and griddata_blockvisibility_reweight,
+ * griddata/gridding.py:260-425).  The flagged imaging weights are gridded on
+ * the image-sized uv grid (cell of a sample: round((u f/c) / cdelt_u + nx/2)
+ * with cdelt_u = 1 / (nx cdelt_x_deg pi/180), likewise v), then every
+ * sample's imaging weight becomes
+ *   GB_WEIGHT_UNIFORM  w (w / G),
+ *   GB_WEIGHT_ROBUST   w (1 + f2 w) / (1 + f2 G), f2 = (5 10^-R)^2 sum(w) / sum(G^2),
+ *   (0 where G <= 0), or for GB_WEIGHT_NATURAL the weight itself.
+ *   uvw_dev       [nrows][3] f64 metres (as stored, no sign flips)
+ *   freq_dev      [nchan] f64 Hz; vis_to_im_dev [nchan] i32 image channel of each
+ *   weight_dev, imaging_weight_dev  [nrows][nchan][npol] f64
+ *   flags_dev     [nrows][nchan][npol] of flags_type, or NULL (GB_FLAGS_NONE)
+ *   cdelt_x_deg, cdelt_y_deg  the image WCS's cdelt[0], cdelt[1] (degrees)
+ *   grid_dev      [nchan_img][npol][ny][nx] f64 scratch: the gridded weights on return
+ *   imaging_weight_out_dev  [nrows][nchan][npol] f64 (may alias neither input)
+ *   sums_dev      [2] f64: sum(G), sum(G^2) on return
+ * Synchronises `stream` (to report) and returns GB_ERR_OUT_OF_GRID when a
+ * sample's cell lies outside the grid (the reference asserts). */
+typedef enum { GB_WEIGHT_NATURAL = 0, GB_WEIGHT_UNIFORM = 1, GB_WEIGHT_ROBUST = 2 } gb_weighting;
+int gb_weight_visibility(const double *uvw_dev, const double *freq_dev, int64_t nrows,
+                         int32_t nchan, int32_t npol, const int32_t *vis_to_im_dev,
+                         int32_t nchan_img, int32_t nx, int32_t ny, double cdelt_x_deg,
+                         double cdelt_y_deg, const double *weight_dev,
+                         const double *imaging_weight_dev, const void *flags_dev,
+                         int32_t flags_type, int32_t weighting, double robustness,
+                         double *grid_dev, double *imaging_weight_out_dev, double *sums_dev,
+                         void *stream);
 
 /* Message for the calling thread's last non-GB_OK status. */
 const char *gb_last_error_string(void);

@@ -22,6 +22,8 @@ GB_ERR_CUDA = 4
 GB_ERR_CUFFT = 5
 GB_ERR_TIMEOUT = 6
 GB_ERR_INTERNAL = 7
+GB_ERR_OUT_OF_GRID = 8
+GB_WEIGHT_NATURAL, GB_WEIGHT_UNIFORM, GB_WEIGHT_ROBUST = 0, 1, 2
 
 GB_FP32 = 0
 GB_FP64 = 1
@@ -92,6 +94,10 @@ SIGNATURES = {
     "gb_plan_bind": (_c.c_int, [_vp, _vp, _c.c_size_t, _vp]),
     "gb_plan_info_get": (_c.c_int, [_vp, _c.POINTER(PlanInfo)]),
     "gb_plan_destroy": (_c.c_int, [_vp]),
+    "gb_weight_visibility": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32, _vp,
+                                        _c.c_int32, _c.c_int32, _c.c_int32, _c.c_double,
+                                        _c.c_double, _vp, _vp, _vp, _c.c_int32, _c.c_int32,
+                                        _c.c_double, _vp, _vp, _vp, _vp]),
     "gb_plan_device_status": (_c.c_int, [_vp, _vp, _c.POINTER(_c.c_int32)]),
     "gb_plan_export_items": (_c.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "gb_plan_ms2dirty": (_c.c_int, [_vp, _vp, _c.c_int32, _vp, _vp, _c.c_int32, _dp,
@@ -130,6 +136,11 @@ class GridderError(RuntimeError):
     """A non-argument failure reported by the C-ABI."""
 
 
+class OutOfGridError(ValueError, AssertionError):
+    """A sample's uv cell lies outside the weighting grid (the reference
+    asserts there, so this is also an AssertionError)."""
+
+
 def load(build_if_missing=True):
     """Load (building first if needed) the shared library."""
     global _lib
@@ -158,6 +169,8 @@ def check(status, what=""):
     text = "%s: %s" % (what, msg) if what else msg
     if status == GB_ERR_INVALID_ARG:
         raise ValueError(text)
+    if status == GB_ERR_OUT_OF_GRID:
+        raise OutOfGridError(text)
     raise GridderError("status %d: %s" % (status, text))
 
 

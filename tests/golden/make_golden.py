@@ -18,7 +18,13 @@ so the functions on this path that are plain numpy are loaded directly:
   file path with stand-in ``astropy`` modules (those three functions do not
   use astropy);
 * ``normalise_sumwt`` -- extracted from
-  ``rascil/processing_components/imaging/base.py`` with ``ast``.
+  ``rascil/processing_components/imaging/base.py`` with ``ast``;
+* ``grid_blockvisibility_weight_to_griddata``,
+  ``griddata_blockvisibility_reweight``, ``convolution_mapping_blockvisibility``
+  and ``spatial_mapping`` -- extracted from
+  ``rascil/processing_components/griddata/gridding.py`` with ``ast`` and run
+  on stand-in BlockVisibility / GridData objects (the uv grid's WCS as the
+  linear map create_griddata_from_image builds).
 
 Outputs go to ``tests/golden/*.npz`` next to this script.
 """
@@ -135,7 +141,138 @@ def main(ref):
     res = ns(_Img(img.copy()), sumwt)["pixels"].data
     numpy.savez_compressed(os.path.join(HERE, "normalise_sumwt.npz"), image=img, sumwt=sumwt,
                            out=res)
+
+    # --- imaging weights: weight gridding + reweighting --------------------------
+    weighting_golden(rascil, rng)
     print("golden vectors written to", HERE)
+
+
+class _LinearWcs:
+    """Linear axes as astropy evaluates them for these grids:
+    pixel = (world - crval) / cdelt + crpix - 1 (origin 0)."""
+
+    def __init__(self, crpix, cdelt, crval):
+        self.crpix = list(crpix)
+        self.cdelt = list(cdelt)
+        self.crval = list(crval)
+
+    def sub(self, axes):
+        i = [a - 1 for a in axes]
+        return _LinearWcs([self.crpix[k] for k in i], [self.cdelt[k] for k in i],
+                          [self.crval[k] for k in i])
+
+    def wcs_world2pix(self, *args):
+        world, origin = args[:-1], args[-1]
+        return [(numpy.asarray(w) - self.crval[k]) / self.cdelt[k] + self.crpix[k] - 1 + origin * 0
+                for k, w in enumerate(world)]
+
+
+def weighting_golden(rascil, rng):
+    """grid_blockvisibility_weight_to_griddata and
+    griddata_blockvisibility_reweight (griddata/gridding.py) on stand-in
+    BlockVisibility / GridData objects carrying exactly the attributes those
+    functions read; the uv grid's WCS is the one create_griddata_from_image
+    (griddata/operations.py:71-107) builds, as a linear _LinearWcs."""
+    path = os.path.join(rascil, "processing_components/griddata/gridding.py")
+    ns = {"numpy": numpy, "GridData": object}
+    for fn in ("convolution_mapping_blockvisibility", "spatial_mapping",
+               "grid_blockvisibility_weight_to_griddata", "griddata_blockvisibility_reweight"):
+        load_function(path, fn, ns)
+    grid_w = ns["grid_blockvisibility_weight_to_griddata"]
+    reweight = ns["griddata_blockvisibility_reweight"]
+
+    nt, nb, nch, npol, npix, nchan_img = 6, 9, 3, 2, 64, 3
+    cell = 2.0e-3
+    freq = numpy.array([1.0e8, 1.1e8, 1.25e8])
+    uvmax = 0.45 / cell  # wavelengths: keep every sample inside the grid
+    uvw = rng.uniform(-1.0, 1.0, (nt, nb, 3)) * numpy.array([1.0, 1.0, 0.2]) \
+        * (uvmax * 299792458.0 / freq.max())
+    weight = rng.uniform(0.5, 2.0, (nt, nb, nch, npol))
+    imaging_weight = weight * rng.uniform(0.8, 1.2, weight.shape)
+    flags = (rng.uniform(0, 1, weight.shape) < 0.1).astype(numpy.int64)
+    # image WCS of a canonical image: RA---SIN cdelt -cell, DEC--SIN +cell (degrees),
+    # frequency axis one channel per visibility channel
+    cdelt_deg = numpy.degrees(cell)
+    d2r = numpy.pi / 180.0
+    cdu = 1.0 / (npix * -cdelt_deg * d2r)
+    cdv = 1.0 / (npix * cdelt_deg * d2r)
+    fwcs = _LinearWcs([1.0, 1.0, 1.0, 1.0], [cdu, cdv, 1.0, 1.0e7], [0.0, 0.0, 1.0, 1.0e8])
+    fwcs.crpix = [npix // 2 + 1, npix // 2 + 1, 1.0, 1.0]
+    fwcs.cdelt[3] = (freq[-1] - freq[0]) / (nchan_img - 1)
+    fwcs.crval[3] = freq[0]
+    k = freq / 299792458.0
+
+    class _FlatArray(numpy.ndarray):
+        """numpy 2 returns a read-only array from nan_to_num(a.flat); the
+        reference was written against numpy 1, where it is a writable copy.
+        .flat here gives that copy (same element order)."""
+
+        @property
+        def flat(self):
+            return numpy.array(self).ravel()
+
+    uvw_lambda = numpy.einsum("tbs,k->tbks", uvw, k).view(_FlatArray)
+
+    class _BVisAcc:
+        def __init__(self, v):
+            self.v = v
+            self.polarisation_frame = "pol"
+
+        @property
+        def flagged_imaging_weight(self):
+            return self.v._d["imaging_weight"].data * (1 - self.v._d["flags"].data)
+
+        @property
+        def flagged_weight(self):
+            return self.v._d["weight"].data * (1 - self.v._d["flags"].data)
+
+    class _BVis:
+        def __init__(self):
+            self._d = {"imaging_weight": types.SimpleNamespace(data=imaging_weight.copy()),
+                       "weight": types.SimpleNamespace(data=weight.copy()),
+                       "flags": types.SimpleNamespace(data=flags.copy())}
+            self.vis = types.SimpleNamespace(shape=weight.shape)
+            self.frequency = types.SimpleNamespace(data=freq)
+            self.uvw_lambda = types.SimpleNamespace(data=uvw_lambda)
+            self.blockvisibility_acc = _BVisAcc(self)
+
+        def __getitem__(self, key):
+            return self._d[key]
+
+    class _GridAcc:
+        def __init__(self, gd):
+            self.polarisation_frame = "pol"
+            self.griddata_wcs = fwcs
+            self.gd = gd
+
+        @property
+        def shape(self):
+            return self.gd._d["pixels"].data.shape
+
+    class _Grid:
+        def __init__(self):
+            self._d = {"pixels": types.SimpleNamespace(
+                data=numpy.zeros((nchan_img, npol, npix, npix), dtype=complex))}
+            self.griddata_acc = _GridAcc(self)
+
+        def __getitem__(self, key):
+            return self._d[key]
+
+    # reweight reads vis.frequency (not .data) for the channel map
+    out = {"uvw": uvw, "freq": freq, "weight": weight, "imaging_weight": imaging_weight,
+           "flags": flags, "npix": npix, "cell": cell, "nchan_img": nchan_img,
+           "wcs_crpix": numpy.array(fwcs.crpix), "wcs_cdelt": numpy.array(fwcs.cdelt),
+           "wcs_crval": numpy.array(fwcs.crval)}
+    for scheme, rob in (("uniform", 0.0), ("robust", 0.5), ("robust", -1.0), ("natural", 0.0)):
+        vis = _BVis()
+        gd, sumwt = grid_w(vis, _Grid())
+        vis.frequency = freq
+        res = reweight(vis, gd, weighting=scheme, robustness=rob)
+        tag = "%s_%g" % (scheme, rob)
+        out["grid_" + tag] = numpy.real(gd["pixels"].data)
+        out["sumwt_" + tag] = sumwt
+        out["imaging_weight_" + tag] = res["imaging_weight"].data
+    numpy.savez_compressed(os.path.join(HERE, "weighting.npz"), **out)
 
 
 if __name__ == "__main__":

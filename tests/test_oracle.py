@@ -93,3 +93,29 @@ def test_c_gridder_plane_subset_sums_to_whole():
     parts = cgridder.grid_items(pr, ms, 2, range(0, k, 2)) + cgridder.grid_items(pr, ms, 2,
                                                                                   range(1, k, 2))
     assert rel_rms(parts, full) < 1e-13
+
+
+def test_weighting_oracle_matches_reference_golden():
+    """oracle/weighting.py reproduces the reference's own
+    grid_blockvisibility_weight_to_griddata + griddata_blockvisibility_reweight
+    (tests/golden/weighting.npz, made by tests/golden/make_golden.py)."""
+    import os
+    import numpy
+    from oracle import weighting as ow
+    d = numpy.load(os.path.join(os.path.dirname(__file__), "golden", "weighting.npz"))
+    npix, cell, nchan_img = int(d["npix"]), float(d["cell"]), int(d["nchan_img"])
+    nt, nb, nch, npol = d["weight"].shape
+    crpix, cdelt, crval = d["wcs_crpix"], d["wcs_cdelt"], d["wcs_crval"]
+    freq = d["freq"]
+    vis_to_im = numpy.round((freq - crval[3]) / cdelt[3] + crpix[3] - 1).astype(int)
+    cdelt_deg = numpy.degrees(cell)
+    sh = (nt * nb, nch, npol)
+    for scheme, rob in (("uniform", 0.0), ("robust", 0.5), ("robust", -1.0), ("natural", 0.0)):
+        tag = "%s_%g" % (scheme, rob)
+        w, grid, sumwt = ow.weight_visibility(
+            d["uvw"], freq, d["weight"].reshape(sh), d["imaging_weight"].reshape(sh),
+            d["flags"].reshape(sh), vis_to_im, nchan_img, npix, npix, -cdelt_deg, cdelt_deg,
+            scheme, rob)
+        numpy.testing.assert_array_equal(grid, d["grid_" + tag])
+        numpy.testing.assert_array_equal(sumwt, d["sumwt_" + tag])
+        numpy.testing.assert_array_equal(w.reshape(d["weight"].shape), d["imaging_weight_" + tag])
