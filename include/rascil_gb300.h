@@ -89,6 +89,17 @@ typedef struct {
   int32_t slab;        /* w-planes per bucket slab; 0 = default                */
   int64_t grid_budget_bytes; /* memory for one batch of w-planes; 0 = default  */
   int32_t fft_mode;    /* gb_fft_mode                                          */
+  /* Tangent-plane phase rotation fused into the plan (RASCIL's
+   * shift_vis_to_image -> phaserotate_visibility, imaging/base.py:67-106,
+   * visibility/base.py:296-357,1248-1264).  s = phase_shift in the plan's
+   * own uvw frame: ms2dirty grids vis * exp(+2 pi i (u s0 + v s1 + w s2)
+   * f/c) (not in PSF mode, whose unit visibilities the reference sets
+   * after its rotation); dirty2ms returns its predictions times
+   * exp(-2 pi i (u s0 + v s1 + w s2) f/c).  For RASCIL's direction cosines
+   * (l, m, n - 1) of the image centre about the visibility phase centre
+   * and ng.py's uvw (u and w negated), s = (-l, m, -(n - 1)).  All zero:
+   * no rotation.                                                          */
+  double phase_shift[3];
 } gb_plan_params;
 
 /* Geometry the planner chose; all host values. */
@@ -292,6 +303,21 @@ int gb_weight_visibility(const double *uvw_dev, const double *freq_dev, int64_t 
                          int32_t flags_type, int32_t weighting, double robustness,
                          double *grid_dev, double *imaging_weight_out_dev, double *sums_dev,
                          void *stream);
+
+/* Tangent-plane phase rotation of visibilities in place, RASCIL's
+ * phaserotate_visibility(tangent=True) (visibility/base.py:296-357) with
+ * the phasor of calculate_blockvisibility_phasor (:1248-1264):
+ *   vis[r][c][p] *= exp(+2 pi i d)   (inverse = 0: times conj(phasor))
+ *   vis[r][c][p] *= exp(-2 pi i d)   (inverse = 1: times phasor)
+ * with d = (uvw[r] f_c / c) . (s_l, s_m, s_n), formed in FP64; s is
+ * (l, m, sqrt(1 - l^2 - m^2) - 1) of the new phase centre about the old.
+ *   uvw_dev [nrows][3] f64 metres; freq_dev [nchan] f64 Hz
+ *   vis_dev [nrows][nchan][npol] complex64 (GB_FP32) or complex128 (GB_FP64)
+ * Asynchronous on `stream`.  invert/predict do not need it: they fuse the
+ * rotation through gb_plan_params.phase_shift. */
+int gb_phase_rotate(const double *uvw_dev, const double *freq_dev, int64_t nrows,
+                    int32_t nchan, int32_t npol, void *vis_dev, int32_t precision, double s_l,
+                    double s_m, double s_n, int32_t inverse, void *stream);
 
 /* Message for the calling thread's last non-GB_OK status. */
 const char *gb_last_error_string(void);

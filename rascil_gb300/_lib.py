@@ -57,6 +57,7 @@ class PlanParams(_c.Structure):
         ("slab", _c.c_int32),
         ("grid_budget_bytes", _c.c_int64),
         ("fft_mode", _c.c_int32),
+        ("phase_shift", _c.c_double * 3),
     ]
 
 
@@ -99,6 +100,9 @@ SIGNATURES = {
                                         _c.c_double, _vp, _vp, _vp, _c.c_int32, _c.c_int32,
                                         _c.c_double, _vp, _vp, _vp, _vp]),
     "gb_plan_device_status": (_c.c_int, [_vp, _vp, _c.POINTER(_c.c_int32)]),
+    "gb_phase_rotate": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32, _vp,
+                                   _c.c_int32, _c.c_double, _c.c_double, _c.c_double,
+                                   _c.c_int32, _vp]),
     "gb_plan_export_items": (_c.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "gb_plan_ms2dirty": (_c.c_int, [_vp, _vp, _c.c_int32, _vp, _vp, _c.c_int32, _dp,
                                     _c.c_int32, _vp, _c.c_int32, _vp, _vp]),

@@ -53,6 +53,8 @@ struct Geom {
   uint32_t nitems;   // R * C
   int B;             // planes per batch
   int nquad;         // quadrature nodes for the w correction
+  int shifted;       // a phase shift is fused into the item factors
+  double shift[3];   // its (u, v, w) coefficients, plan uvw frame
 };
 
 // Item record in bucket order.  `loc` packs the item's first support cell
@@ -140,6 +142,27 @@ __host__ __device__ inline double gb_div(double a, double b) {
 #else
   return a / b;
 #endif
+}
+
+// Turns of an item's rotation factor exp(-2 pi i turns), reduced to
+// [-1/2, 1/2]: the w-centring term w tc and, when `shift`, minus the fused
+// phase shift (u, v, w) . s (wavelengths).  Formed in FP64 before the
+// reduction; the FP32 form rounds only the reduced value.
+__host__ __device__ inline double item_turns(const Geom &g, const double *uvw,
+                                             const double *freq, uint32_t i, bool shift) {
+  const uint32_t r = i / (uint32_t)g.C;
+  const uint32_t c = i - r * (uint32_t)g.C;
+  const double k = gb_div(freq[c], kSpeedOfLight);
+  const double w = gb_mul(uvw[3 * (size_t)r + 2], k);
+  double t = g.do_w ? gb_mul(w, g.tc) : 0.0;
+  if (shift) {
+    const double u = gb_mul(uvw[3 * (size_t)r + 0], k);
+    const double v = gb_mul(uvw[3 * (size_t)r + 1], k);
+    const double d = gb_add(gb_add(gb_mul(u, g.shift[0]), gb_mul(v, g.shift[1])),
+                            gb_mul(w, g.shift[2]));
+    t = gb_sub(t, d);
+  }
+  return gb_sub(t, rint(t));
 }
 
 __host__ __device__ inline void item_coord(const Geom &g, const double *uvw,

@@ -28,8 +28,8 @@ __global__ void __launch_bounds__(kThreads)
     k_prep_vis(const Geom g, const typename Traits<R>::Item *__restrict__ items,
                const typename Traits<R>::C *__restrict__ vis, int npv,
                const R *__restrict__ wgt, const void *__restrict__ flags, int ftype,
-               const PolMat pm, int psf, typename Traits<R>::C *__restrict__ cvis,
-               double *__restrict__ sumwt) {
+               const PolMat pm, int psf, const double *__restrict__ coords,
+               typename Traits<R>::C *__restrict__ cvis, double *__restrict__ sumwt) {
   using C = typename Traits<R>::C;
   double wsum[NP];
 #pragma unroll
@@ -38,6 +38,15 @@ __global__ void __launch_bounds__(kThreads)
   for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < g.nitems; j += stride) {
     const auto it = items[j];
     const size_t base = (size_t)it.idx * npv;
+    // PSF of a phase-shifted plan: unit visibilities carry the w-centring
+    // factor alone (the reference rotates before it sets them to one)
+    auto ph = it.ph;
+    if (coords) {
+      R s, c;
+      sincos_2pi((R)item_turns(g, coords, coords + 3 * (size_t)g.R, it.idx, false), &s, &c);
+      ph.x = c;
+      ph.y = -s;
+    }
     R m[4];
     for (int q = 0; q < 4; ++q) m[q] = (R)1;
     if (ftype == GB_FLAGS_U8) {
@@ -88,8 +97,8 @@ __global__ void __launch_bounds__(kThreads)
       wsum[p] += (double)w;
       const R re = out[p].x * w, im = out[p].y * w;
       C o;
-      o.x = re * it.ph.x - im * it.ph.y;
-      o.y = re * it.ph.y + im * it.ph.x;
+      o.x = re * ph.x - im * ph.y;
+      o.y = re * ph.y + im * ph.x;
       cvis[(size_t)j * NP + p] = o;
     }
   }
@@ -478,7 +487,8 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
     ProfScope ps(kProfPrepVis, s, per * (double)g.nitems);
     k_prep_vis<R, NP><<<item_blocks, kThreads, 0, s>>>(
         g, items, reinterpret_cast<const C *>(vis), npv, reinterpret_cast<const R *>(wgt), flags,
-        ftype, pm, psf, cvis, sumwt);
+        ftype, pm, psf,
+        psf && g.shifted ? p->at<const double>(p->off_coords) : nullptr, cvis, sumwt);
     GB_LAUNCH_CHECK("k_prep_vis");
   }
   const size_t plane = (size_t)g.ngx * g.ngy;

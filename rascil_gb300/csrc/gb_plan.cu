@@ -198,6 +198,14 @@ int plan_geometry(const gb_plan_params *p, double w_lo, double w_hi, Geom &g) {
   g.C = p->nchan;
   g.NP = p->npol;
   g.nitems = (uint32_t)nitems;
+  for (int k = 0; k < 3; ++k) {
+    if (!std::isfinite(p->phase_shift[k])) {
+      set_error("phase_shift[%d] = %g is not finite", k, p->phase_shift[k]);
+      return GB_ERR_INVALID_ARG;
+    }
+    g.shift[k] = p->phase_shift[k];
+  }
+  g.shifted = g.shift[0] != 0.0 || g.shift[1] != 0.0 || g.shift[2] != 0.0;
   const int64_t budget =
       p->grid_budget_bytes > 0 ? p->grid_budget_bytes : (int64_t)32 << 30;
   const int64_t per_plane =
@@ -387,10 +395,9 @@ __global__ void k_scatter(const Geom g, const double *__restrict__ uvw,
     it.du = (R)o.du;
     it.dv = (R)o.dv;
     it.dwf = (R)o.dwf;
-    if (g.do_w) {
-      // exp(-2 pi i w tc), phase reduced in FP64 before the sincos
-      double turns = o.w * g.tc;
-      turns -= rint(turns);
+    if (g.do_w || g.shifted) {
+      // exp(-2 pi i (w tc - (u, v, w) . shift)), reduced in FP64 before the sincos
+      const double turns = item_turns(g, uvw, freq, (uint32_t)i, g.shifted);
       R s, c;
       sincos_2pi((R)turns, &s, &c);
       it.ph.x = c;
@@ -668,6 +675,9 @@ static int layout_workspace(gb_plan *p) {
   off = align_up(off + (p->col_fft ? (size_t)g.nplanes * g.ntv : 0));
   p->off_tables = off;
   off = align_up(off + 8 * ((size_t)g.nx + g.ny + 2 * kMaxQuad));
+  // shifted plans keep uvw and freq: a PSF call rebuilds the unshifted factor
+  p->off_coords = off;
+  off = align_up(off + (g.shifted ? 8 * (3 * (size_t)g.R + g.C) : 0));
   p->off_counters = off;
   off = align_up(off + 4 * (size_t)(2 * p->nbatches + 8));
   p->off_fftwork = off;
@@ -724,6 +734,12 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   const double ni = (double)g.nitems, rows = (double)g.R * 24.0 + 8.0 * g.C;
   GB_CUDA(cudaMemsetAsync(counts, 0, 4 * (size_t)(nb + 1), s));
   GB_CUDA(cudaMemsetAsync(p->status_word(), 0, 4, s));
+  if (g.shifted) {
+    GB_CUDA(cudaMemcpyAsync(p->at<double>(p->off_coords), p->uvw, 24 * (size_t)g.R,
+                            cudaMemcpyDeviceToDevice, s));
+    GB_CUDA(cudaMemcpyAsync(p->at<double>(p->off_coords) + 3 * (size_t)g.R, p->freq,
+                            8 * (size_t)g.C, cudaMemcpyDeviceToDevice, s));
+  }
   {
     ProfScope ps(kProfCountKernel, s, rows + 8.0 * ni);
     k_count<<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, counts, keys, ranks);

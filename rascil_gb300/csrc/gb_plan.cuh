@@ -45,6 +45,7 @@ struct gb_plan {
   size_t off_rowmask = 0, off_twx = 0;
   int row_blocks = 0;
   size_t off_tprime = 0;  // [ny][nx] float64: n - 1 - tc per pixel (w-stacking)
+  size_t off_coords = 0;  // shifted plans: [R][3] uvw then [C] freq, float64
   // column mode: [ny][nx] w-screen phases as 64-bit fixed-point turns
   // (A, D), plane k's phase = A + k D mod 1; [ngy] exp(+2 pi i m / ngy)
   size_t off_screen = 0, off_twn = 0;

@@ -11,7 +11,7 @@ import logging
 
 import numpy
 
-from ..data_models import SPEED_OF_LIGHT, SkyDirection, copy_visibility
+from ..data_models import SkyDirection, copy_visibility
 
 log = logging.getLogger("rascil-logger")
 
@@ -78,27 +78,103 @@ def phase_rotation_needed(bvis, im):
     return separation(bvis.phasecentre, pc) > 1e-15, pc
 
 
-def shift_vis_to_image(bvis, im, tangent=True, inverse=False):
-    """Phase-rotate vis to the image phase centre (or back if ``inverse``)."""
-    if not tangent:
-        raise NotImplementedError("only tangent-plane rotation is supported")
+def phasor_direction(newphasecentre, phasecentre):
+    """(l, m, sqrt(1 - l^2 - m^2) - 1) of ``newphasecentre`` about
+    ``phasecentre`` (``visibility/base.py:1257-1258``), or None when the
+    reference skips the rotation (``|n - 1| < 1e-15``, ``:311-314``)."""
+    l, m, n = lmn_of(newphasecentre, phasecentre)
+    if abs(n - 1.0) < 1e-15:
+        return None
+    return float(l), float(m), float(numpy.sqrt(1.0 - l * l - m * m) - 1.0)
+
+
+def fused_phase_shift(bvis, im):
+    """What ``shift_vis_to_image(bvis, im, tangent=True)`` does, as the
+    gridder plan's fused phase shift: ``(rotates, shift)`` with ``shift`` in
+    the plan's uvw frame (u and w negated, as ng.py hands uvw to the
+    gridder).  ``rotates`` says whether the reference would re-label the
+    visibilities' phase centre (the separation test of ``imaging/base.py:90``)."""
     needed, pc = phase_rotation_needed(bvis, im)
     if not needed:
-        return bvis
-    l, m, n = lmn_of(pc, bvis.phasecentre)
-    if abs(n - 1.0) < 1e-15 and abs(l) < 1e-15 and abs(m) < 1e-15:
-        return bvis
-    new = copy_visibility(bvis)
-    s = numpy.array([l, m, n - 1.0])
-    f = new.frequency.data / SPEED_OF_LIGHT
-    phase = numpy.einsum("tbs,s->tb", new.uvw.data, s)[..., None] * f
-    phasor = numpy.exp(-2j * numpy.pi * phase)[..., None]
-    if inverse:
-        new["vis"].data = new["vis"].data * phasor
+        return False, (0.0, 0.0, 0.0)
+    s = phasor_direction(pc, bvis.phasecentre)
+    if s is None:
+        return True, (0.0, 0.0, 0.0)
+    return True, (-s[0], s[1], -s[2])
+
+
+def _rotate_uvw(uvw, old, new):
+    """uvw at phase centre ``old`` -> uvw at ``new`` through the XYZ frame
+    (``visibility/base.py:331-355``: ``uvw_to_xyz`` with ha = -ra_old,
+    ``xyz_to_uvw`` with ha = -ra_new); rotations of [R][3] coordinates."""
+    from ..simulation import xyz_to_uvw
+    ra0, dec0 = _ra_dec(old)
+    ra1, dec1 = _ra_dec(new)
+    u, v, w = uvw[:, 0], uvw[:, 1], uvw[:, 2]
+    h, d = -ra0, dec0
+    # inverse of xyz_to_uvw(., h, d)
+    z = w * numpy.sin(d) + v * numpy.cos(d)
+    v0 = v * numpy.sin(d) - w * numpy.cos(d)
+    x = u * numpy.cos(h) + v0 * numpy.sin(h)
+    y = v0 * numpy.cos(h) - u * numpy.sin(h)
+    return xyz_to_uvw(numpy.stack([x, y, z], axis=-1), -ra1, dec1)
+
+
+def phaserotate_visibility(vis, newphasecentre, tangent=True, inverse=False, **kwargs):
+    """Phase-rotate to a new phase centre (``visibility/base.py:296-357``):
+    a copy whose visibilities are multiplied, on the GPU
+    (``gb_phase_rotate``), by conj(phasor) (or by the phasor if
+    ``inverse``), phasor = exp(-2 pi i uvw_lambda . s).  With
+    ``tangent=False`` the uvw are also rotated to the new phase centre and
+    the copy's phase centre updated, as the reference does."""
+    s = phasor_direction(newphasecentre, vis.phasecentre)
+    if s is None:
+        return vis
+    import torch
+
+    from .. import _lib
+    data = vis["vis"].data
+    if data.dtype == numpy.complex128:
+        prec, cdt = _lib.GB_FP64, torch.complex128
+    elif data.dtype == numpy.complex64:
+        prec, cdt = _lib.GB_FP32, torch.complex64
     else:
-        new["vis"].data = new["vis"].data * numpy.conj(phasor)
-    new.attrs["phasecentre"] = im.image_acc.phasecentre
-    return new
+        raise TypeError("vis must be complex64 or complex128, not %s" % data.dtype)
+    nrows, nbl, nchan, npol = data.shape
+    device = torch.device(kwargs.get("device", "cuda"))
+
+    def up(x):
+        t = torch.from_numpy(numpy.ascontiguousarray(x))
+        return t.to(device=device, non_blocking=t.is_pinned())
+
+    with torch.cuda.device(device):
+        dv = up(data)
+        uvw = up(numpy.asarray(vis.uvw.data, dtype=numpy.float64).reshape(-1, 3))
+        freq = up(numpy.asarray(vis.frequency.data, dtype=numpy.float64))
+        stream = torch.cuda.current_stream(device).cuda_stream
+        _lib.check(_lib.load().gb_phase_rotate(
+            uvw.data_ptr(), freq.data_ptr(), nrows * nbl, nchan, npol, dv.data_ptr(), prec,
+            s[0], s[1], s[2], 1 if inverse else 0, stream), "phaserotate_visibility")
+        host = torch.empty(dv.shape, dtype=cdt, pin_memory=True)
+        host.copy_(dv)
+    newvis = copy_visibility(vis, vis=host.numpy())
+    if not tangent:
+        uvw = numpy.asarray(vis.uvw.data, dtype=numpy.float64).reshape(-1, 3)
+        newvis["uvw"].data[...] = _rotate_uvw(uvw, vis.phasecentre,
+                                              newphasecentre).reshape(vis.uvw.data.shape)
+        newvis.attrs["phasecentre"] = newphasecentre
+    return newvis
+
+
+def shift_vis_to_image(bvis, im, tangent=True, inverse=False, **kwargs):
+    """Phase-rotate vis to the image phase centre, or back if ``inverse``
+    (``imaging/base.py:67-106``).  invert_ng / predict_ng fuse this step
+    into the gridder (``fused_phase_shift``); this is the standalone form."""
+    needed, pc = phase_rotation_needed(bvis, im)
+    if needed:
+        bvis = phaserotate_visibility(bvis, pc, tangent=tangent, inverse=inverse, **kwargs)
+        bvis.attrs["phasecentre"] = im.image_acc.phasecentre
+    return bvis
 
 
 def normalise_sumwt(im, sumwt):

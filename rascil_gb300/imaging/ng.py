@@ -14,6 +14,10 @@ Same signatures, keyword arguments, defaults and results as
 * MFS (``ng.py:227-250``): one plan over all channels.  Per-channel
   (``ng.py:251-277``): one plan per image channel over the visibility
   channels that map to it (their sum is what ng.py accumulates);
+* ``shift_vis_to_image`` (``ng.py:129-130,169-170``, a tangent-plane phase
+  rotation when the image centre is not the visibilities' phase centre) is
+  fused into the plan's per-item phase factors, so it costs no pass and no
+  copy of the visibilities;
 * images accumulate and are normalised by sumwt on the device; host
   arrays in page-locked memory move by direct DMA, and results come back
   into page-locked arrays (torch's host caching allocator).
@@ -33,7 +37,7 @@ import torch
 from ..data_models import copy_visibility
 from ..polarisation import conversion_matrix
 from ..wgridder import Plan
-from .base import image_is_canonical, shift_vis_to_image
+from .base import fused_phase_shift, image_is_canonical
 
 log = logging.getLogger("rascil-logger")
 
@@ -111,9 +115,9 @@ def _retire(plan):
         _spare_ws[:] = keep[-1:]
 
 
-def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision):
+def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, shift):
     plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=npol,
-                precision=precision, bind=False)
+                precision=precision, bind=False, phase_shift=shift)
     need = max(plan.workspace_bytes, 256)
     ws = None
     with _plan_lock:
@@ -127,9 +131,9 @@ def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision):
     return plan
 
 
-def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision):
+def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, shift):
     key = (uvw.device, tuple(uvw.shape), tuple(f.cpu().tolist()), nx, ny, float(pixsize),
-           float(epsilon), bool(do_wstacking), int(npol), precision)
+           float(epsilon), bool(do_wstacking), int(npol), precision, tuple(shift))
     if _cache_on():
         with _plan_lock:
             hit = _plan_cache.pop(key, None)
@@ -137,7 +141,8 @@ def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precisi
             if torch.equal(hit[0], uvw):
                 return key, hit
             _retire(hit[1])
-    return key, (uvw, _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision))
+    return key, (uvw, _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision,
+                                shift))
 
 
 def _checkin_plan(key, entry):
@@ -183,6 +188,8 @@ def predict_ng(bvis, model, **kwargs):
     assert m_npol == vnpol
     pixsize = abs(numpy.radians(model.image_acc.wcs.wcs.cdelt[0]))
     vis_to_im = _vis_to_im(model, freq)
+    # shift_vis_to_image(..., inverse=True) of ng.py:130, fused into the plan
+    rotates, shift = fused_phase_shift(bvis, model)
     polmat = conversion_matrix(model.image_acc.polarisation_frame,
                                bvis.blockvisibility_acc.polarisation_frame)
     pm = None if numpy.array_equal(polmat, numpy.eye(vnpol)) else polmat
@@ -196,7 +203,7 @@ def predict_ng(bvis, model, **kwargs):
     for ichan, chans in groups:
         f = torch.from_numpy(numpy.ascontiguousarray(freq[chans])).to(device)
         key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, m_npol,
-                                    precision)
+                                    precision, shift)
         try:
             img = _to_device(pixels[ichan], rdt, device)
             vis = entry[1].dirty2ms(img, polmat=pm, npol_vis=vnpol, layout="yx")
@@ -218,7 +225,9 @@ def predict_ng(bvis, model, **kwargs):
     # ng.py:56 deep-copies the input and zeroes vis; the copy gets the
     # predicted visibilities directly instead
     newbvis = copy_visibility(bvis, vis=result)
-    return shift_vis_to_image(newbvis, model, tangent=True, inverse=True)
+    if rotates:
+        newbvis.attrs["phasecentre"] = model.image_acc.phasecentre
+    return newbvis
 
 
 def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
@@ -232,7 +241,10 @@ def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
     cdt = torch.complex128 if precision == "fp64" else torch.complex64
     rdt = torch.float64 if precision == "fp64" else torch.float32
 
-    sbvis = shift_vis_to_image(bvis, im, tangent=True, inverse=False)
+    # shift_vis_to_image of ng.py:169-170, fused into the plan: the gridder
+    # multiplies by the phase factor, so the visibilities are not copied
+    _, shift = fused_phase_shift(bvis, im)
+    sbvis = bvis
     freq = numpy.asarray(sbvis.frequency.data, dtype=numpy.float64)
     nrows, nbaselines, vnchan, vnpol = sbvis.vis.shape
     nchan, npol, ny, nx = im["pixels"].data.shape
@@ -268,7 +280,7 @@ def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
             return t if (t is None or whole) else t[:, sel, :].contiguous()
 
         key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol,
-                                    precision)
+                                    precision, shift)
         try:
             dirty, sw = entry[1].ms2dirty(pick(vis), wgt=pick(wgt), flags=pick(flags),
                                           polmat=pm, psf=dopsf, layout="yx", sumwt=True)

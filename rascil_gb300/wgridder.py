@@ -61,11 +61,16 @@ class Plan:
         FP32 form, power-of-two grid height), "columns" (require them) or
         "cufft2d" (batched 2-D cuFFT plans); ``info["fft_mode"]`` reports
         the one in use (2 = columns, 1 = cufft2d)
+    :param phase_shift: (s0, s1, s2) of a tangent-plane phase rotation fused
+        into the plan's per-item factors: ms2dirty grids vis times
+        exp(+2 pi i (u s0 + v s1 + w s2) f/c) (not for a PSF), dirty2ms
+        returns predictions times exp(-2 pi i ...); uvw as given to the plan
     """
 
     def __init__(self, uvw, freq, npix_x, npix_y, pixsize_x, pixsize_y, epsilon,
                  do_wstacking, npol=1, precision="fp32", sigma=0.0, support=0, tile=0,
-                 slab=0, grid_budget_bytes=0, bind=True, fft_mode="auto"):
+                 slab=0, grid_budget_bytes=0, bind=True, fft_mode="auto",
+                 phase_shift=(0.0, 0.0, 0.0)):
         lib = _lib.load()
         _require_cuda(uvw, "uvw")
         _require_cuda(freq, "freq")
@@ -105,6 +110,11 @@ class Plan:
         p.slab = int(slab)
         p.grid_budget_bytes = int(grid_budget_bytes)
         p.fft_mode = _FFT_MODE[fft_mode]
+        shift = [float(x) for x in phase_shift]
+        if len(shift) != 3:
+            raise ValueError("phase_shift must hold three coefficients")
+        p.phase_shift[:] = shift
+        self.phase_shift = tuple(shift)
         self._params = p
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):

@@ -24,11 +24,17 @@ so the functions on this path that are plain numpy are loaded directly:
   and ``spatial_mapping`` -- extracted from
   ``rascil/processing_components/griddata/gridding.py`` with ``ast`` and run
   on stand-in BlockVisibility / GridData objects (the uv grid's WCS as the
-  linear map create_griddata_from_image builds).
+  linear map create_griddata_from_image builds);
+* ``phaserotate_visibility`` and ``calculate_blockvisibility_phasor`` --
+  extracted from ``rascil/processing_components/visibility/base.py`` with
+  ``ast`` and run on a stand-in BlockVisibility, with the reference's
+  ``uvw_to_xyz`` / ``xyz_to_uvw`` and a direction-cosine stand-in for
+  astropy's ``skycoord_to_lmn``.
 
 Outputs go to ``tests/golden/*.npz`` next to this script.
 """
 import ast
+import copy
 import importlib.util
 import logging
 import os
@@ -144,6 +150,9 @@ def main(ref):
 
     # --- imaging weights: weight gridding + reweighting --------------------------
     weighting_golden(rascil, rng)
+
+    # --- phase rotation ----------------------------------------------------------
+    rotation_golden(rascil, cs, rng)
     print("golden vectors written to", HERE)
 
 
@@ -273,6 +282,91 @@ def weighting_golden(rascil, rng):
         out["sumwt_" + tag] = sumwt
         out["imaging_weight_" + tag] = res["imaging_weight"].data
     numpy.savez_compressed(os.path.join(HERE, "weighting.npz"), **out)
+
+
+
+def rotation_golden(rascil, cs, rng):
+    """phaserotate_visibility with its phasor calculate_blockvisibility_phasor
+    (visibility/base.py:296-357,1248-1264) on a stand-in BlockVisibility
+    carrying exactly the attributes they read, with the reference's own
+    uvw_to_xyz / xyz_to_uvw (util/coordinate_support.py).  skycoord_to_lmn
+    (astropy) is replaced by the direction-cosine formula; the (l, m, n - 1)
+    it gave are stored with the vectors, so a test can use the same ones."""
+    path = os.path.join(rascil, "processing_components/visibility/base.py")
+    lmn_used = {}
+
+    def skycoord_to_lmn(pos, centre):
+        ra, dec, ra0, dec0 = pos.ra.rad, pos.dec.rad, centre.ra.rad, centre.dec.rad
+        l = numpy.cos(dec) * numpy.sin(ra - ra0)
+        m = numpy.sin(dec) * numpy.cos(dec0) - numpy.cos(dec) * numpy.sin(dec0) * numpy.cos(ra - ra0)
+        n = numpy.sin(dec) * numpy.sin(dec0) + numpy.cos(dec) * numpy.cos(dec0) * numpy.cos(ra - ra0)
+        lmn_used["lmn"] = (l, m, n - 1.0)
+        return l, m, n - 1.0
+
+    def uvw_lambda(vis):
+        vis.uvw_lambda.data = numpy.einsum("tbs,k->tbks", vis.uvw.data,
+                                           vis.frequency.data / 299792458.0)
+        return vis
+
+    ns = {"numpy": numpy, "BlockVisibility": object, "SkyCoord": object,
+          "skycoord_to_lmn": skycoord_to_lmn, "copy_visibility": copy.deepcopy,
+          "uvw_to_xyz": cs.uvw_to_xyz, "xyz_to_uvw": cs.xyz_to_uvw,
+          "calculate_blockvisibility_uvw_lambda": uvw_lambda}
+    for fn in ("calculate_blockvisibility_phasor", "phaserotate_visibility"):
+        load_function(path, fn, ns)
+    rotate = ns["phaserotate_visibility"]
+
+    class _Dir:
+        def __init__(self, ra, dec):
+            self.ra = types.SimpleNamespace(rad=ra)
+            self.dec = types.SimpleNamespace(rad=dec)
+
+    class _Arr:
+        def __init__(self, a):
+            self.data = a
+
+        @property
+        def shape(self):
+            return self.data.shape
+
+    class _BVis:
+        def __init__(self, vis, uvw, freq, pc):
+            self._v = {"vis": _Arr(vis), "uvw": _Arr(uvw)}
+            self.frequency = _Arr(freq)
+            self.uvw_lambda = _Arr(None)
+            self.attrs = {"phasecentre": pc}
+            uvw_lambda(self)
+
+        def __getitem__(self, k):
+            return self._v[k]
+
+        @property
+        def uvw(self):
+            return self._v["uvw"]
+
+        @property
+        def vis(self):
+            return self._v["vis"]
+
+        @property
+        def phasecentre(self):
+            return self.attrs["phasecentre"]
+
+    nt, nb, nch, npol = 3, 5, 4, 2
+    freq = numpy.linspace(1.0e8, 1.3e8, nch)
+    uvw = rng.uniform(-2000.0, 2000.0, (nt, nb, 3)) * numpy.array([1.0, 1.0, 0.15])
+    vis = rng.normal(size=(nt, nb, nch, npol)) + 1j * rng.normal(size=(nt, nb, nch, npol))
+    pc = (0.3, -0.6)
+    new = (0.317, -0.585)
+    out = dict(uvw=uvw, freq=freq, vis=vis, pc=numpy.array(pc), new=numpy.array(new))
+    for tag, tangent, inverse in (("fwd", True, False), ("inv", True, True),
+                                  ("fwd_nt", False, False), ("inv_nt", False, True)):
+        b = _BVis(vis.copy(), uvw.copy(), freq, _Dir(*pc))
+        r = rotate(b, _Dir(*new), tangent=tangent, inverse=inverse)
+        out["vis_" + tag] = r["vis"].data
+        out["uvw_" + tag] = r.uvw.data
+    out["lmn"] = numpy.array(lmn_used["lmn"])
+    numpy.savez_compressed(os.path.join(HERE, "rotation.npz"), **out)
 
 
 if __name__ == "__main__":

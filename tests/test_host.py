@@ -90,27 +90,78 @@ def test_image_wcs_and_phase_centre():
     numpy.testing.assert_allclose(ch, 0.0)
 
 
-def test_phase_rotation_to_offset_image_centre():
-    """shift_vis_to_image multiplies by conj(exp(-2 pi i uvw_lambda.(l, m, n-1)))
-    of the image centre (visibility/base.py:296-357,1248-1264)."""
+def test_lmn_known_answers():
+    """skycoord_to_lmn's known answers (reference
+    tests/processing_components/test_coordinate_support.py:139-155), as
+    (l, m, n - 1)."""
+    from rascil_gb300.data_models import SkyDirection
+    from rascil_gb300.imaging.base import lmn_of
+    d = numpy.radians
+    centre, north, south = SkyDirection(0, 0), SkyDirection(0, d(90)), SkyDirection(0, d(-90))
+    east, west = SkyDirection(d(90), 0), SkyDirection(d(-90), 0)
+    cases = [(centre, centre, (0, 0, 0)), (north, centre, (0, 1, -1)),
+             (south, centre, (0, -1, -1)), (south, north, (0, 0, -2)),
+             (east, centre, (1, 0, -1)), (west, centre, (-1, 0, -1)),
+             (centre, west, (1, 0, -1)), (north, west, (0, 1, -1)),
+             (south, west, (0, -1, -1)), (north, east, (0, 1, -1)),
+             (south, east, (0, -1, -1))]
+    for pos, ctr, want in cases:
+        l, m, n = lmn_of(pos, ctr)
+        numpy.testing.assert_allclose((l, m, n - 1.0), want, atol=1e-14)
+
+
+def test_uvw_rotation_matches_reference_golden():
+    """tangent=False uvw rotation (visibility/base.py:331-355, the
+    reference's uvw_to_xyz / xyz_to_uvw)."""
+    from rascil_gb300.data_models import SkyDirection
+    from rascil_gb300.imaging.base import _rotate_uvw
+    g = numpy.load(os.path.join(GOLDEN, "rotation.npz"))
+    got = _rotate_uvw(g["uvw"].reshape(-1, 3), SkyDirection(*g["pc"]), SkyDirection(*g["new"]))
+    numpy.testing.assert_allclose(got.reshape(g["uvw"].shape), g["uvw_fwd_nt"], rtol=0,
+                                  atol=1e-9)
+
+
+def test_phase_rotation_property_of_rotated_uvw():
+    """The reference's test_phase_rotate (test_coordinate_support.py:157-193):
+    a point source seen from phase centre A, times the phasor of A about B
+    on B's uvw, equals the same source seen from B."""
+    from oracle.rotation import simulate_point
+    from rascil_gb300.data_models import SkyDirection
+    from rascil_gb300.imaging.base import _rotate_uvw, lmn_of
+    uvw = numpy.array([(1.0, 0, 0), (0, 1.0, 0), (0, 0, 1.0)])
+    d = numpy.radians
+    pos = [SkyDirection(d(17), d(35)), SkyDirection(d(17), d(30)), SkyDirection(d(12), d(30)),
+           SkyDirection(d(11), d(35)), SkyDirection(d(51), d(35)), SkyDirection(d(15), d(70))]
+    for pc in pos:
+        for new in pos:
+            uvw_r = _rotate_uvw(uvw, pc, new)
+            lp, mp, _ = lmn_of(pc, new)
+            ph = simulate_point(uvw_r, lp, mp)
+            for src in pos:
+                l, m, _ = lmn_of(src, pc)
+                lr, mr, _ = lmn_of(src, new)
+                numpy.testing.assert_allclose(simulate_point(uvw, l, m) * ph,
+                                              simulate_point(uvw_r, lr, mr), atol=1e-10)
+
+
+def test_fused_phase_shift_is_the_plan_frame_direction():
+    """invert_ng / predict_ng fuse shift_vis_to_image into the plan: the
+    shift is (-l, m, -(sqrt(1 - l^2 - m^2) - 1)) because ng.py hands the
+    gridder uvw with u and w negated; none when the centres agree."""
     from rascil_gb300 import simulation as sim
     from rascil_gb300.data_models import SkyDirection
-    from rascil_gb300.imaging.base import lmn_of, shift_vis_to_image
+    from rascil_gb300.imaging.base import fused_phase_shift, lmn_of
     uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
     b = sim.make_blockvisibility(uvw, f, pc, cfg)
-    b["vis"].data[...] = 1.0
+    im = sim.model_image(cfg, ([], [], [], [], []), pc, f)
+    assert fused_phase_shift(b, im) == (False, (0.0, 0.0, 0.0))
     off = SkyDirection(pc.ra.rad + 0.01, pc.dec.rad - 0.005)
-    im = sim.model_image(cfg, sim.sources(cfg), off, f)
-    s = shift_vis_to_image(b, im, tangent=True, inverse=False)
-    l, m, n = lmn_of(off, pc)
-    ph = numpy.exp(2j * numpy.pi * (uvw @ numpy.array([l, m, n - 1.0]))[..., None]
-                   * f / 299792458.0)
-    numpy.testing.assert_allclose(s["vis"].data[..., 0], ph, rtol=0, atol=1e-12)
-    # the inverse (applied to unshifted data, as predict_ng does) is the conjugate
-    inv = shift_vis_to_image(b, im, tangent=True, inverse=True)
-    numpy.testing.assert_allclose(inv["vis"].data[..., 0], numpy.conj(ph), rtol=0, atol=1e-12)
-    # after a shift the phase centres agree and a second shift is a no-op
-    assert shift_vis_to_image(s, im, tangent=True, inverse=True) is s
+    im = sim.model_image(cfg, ([], [], [], [], []), off, f)
+    rot, s = fused_phase_shift(b, im)
+    l, m, _ = lmn_of(off, pc)
+    assert rot
+    numpy.testing.assert_allclose(s, (-l, m, -(numpy.sqrt(1 - l * l - m * m) - 1.0)),
+                                  rtol=1e-14, atol=0)
 
 
 def _header_functions():
