@@ -41,7 +41,7 @@ from .base import fused_phase_shift, image_is_canonical
 
 log = logging.getLogger("rascil-logger")
 
-__all__ = ["predict_ng", "invert_ng", "predict_gb", "invert_gb", "clear_plan_cache"]
+__all__ = ["predict_ng", "invert_ng", "residual_ng", "predict_gb", "invert_gb", "clear_plan_cache"]
 
 
 def get_parameter(kwargs, key, default=None):
@@ -93,8 +93,14 @@ def _to_host(t, dtype):
 # uploaded are equal, element for element on the device, to the plan's own.
 # A plan in use is checked out of the cache, so concurrent callers never
 # share one.  RASCIL_GB300_PLAN_CACHE=0 disables it.
+#
+# Callers may run on different CUDA streams (the list workflows run one per
+# worker thread): a plan or workspace handed back carries an event recorded
+# on its last user's stream, the next user's stream waits on it, and every
+# stream that uses a workspace is recorded on the tensor so the caching
+# allocator never reuses it under pending work.
 _plan_cache = {}
-_spare_ws = []  # at most one device workspace of a closed plan, reused by the next
+_spare_ws = []  # at most one (workspace, event) of a closed plan, reused by the next
 _plan_lock = threading.Lock()
 
 
@@ -102,7 +108,22 @@ def _cache_on():
     return os.environ.get("RASCIL_GB300_PLAN_CACHE", "1") != "0"
 
 
-def _retire(plan):
+def _mark_used(ws, event=None):
+    """The current stream is about to use ``ws``: order it after ``event``
+    and keep the allocator from recycling ``ws`` before this stream is done."""
+    stream = torch.cuda.current_stream(ws.device)
+    if event is not None:
+        stream.wait_event(event)
+    ws.record_stream(stream)
+
+
+def _done_event(device):
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream(device))
+    return ev
+
+
+def _retire(plan, event):
     """Close a plan and keep its workspace for the next plan (a multi-GB
     buffer; allocating it anew each call costs more than the transfers)."""
     ws = plan.workspace
@@ -110,8 +131,8 @@ def _retire(plan):
     if ws is None:
         return
     with _plan_lock:
-        keep = [w for w in _spare_ws + [ws] if w.device == ws.device]
-        keep.sort(key=lambda w: w.numel())
+        keep = [w for w in _spare_ws + [(ws, event)] if w[0].device == ws.device]
+        keep.sort(key=lambda w: w[0].numel())
         _spare_ws[:] = keep[-1:]
 
 
@@ -119,42 +140,53 @@ def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, s
     plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=npol,
                 precision=precision, bind=False, phase_shift=shift)
     need = max(plan.workspace_bytes, 256)
-    ws = None
+    spare = None
     with _plan_lock:
-        for i, w in enumerate(_spare_ws):
+        for i, (w, _) in enumerate(_spare_ws):
             if w.device == uvw.device and w.numel() >= need:
-                ws = _spare_ws.pop(i)
+                spare = _spare_ws.pop(i)
                 break
-    if ws is None:
+    if spare is None:
         ws = torch.empty(need, dtype=torch.uint8, device=uvw.device)
+    else:
+        ws = spare[0]
+        _mark_used(ws, spare[1])
     plan.bind(ws)
     return plan
 
 
 def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, shift):
+    """(key, (uvw, plan)) for the current stream: the cached plan when it
+    fits, else a new one."""
     key = (uvw.device, tuple(uvw.shape), tuple(f.cpu().tolist()), nx, ny, float(pixsize),
            float(epsilon), bool(do_wstacking), int(npol), precision, tuple(shift))
     if _cache_on():
         with _plan_lock:
             hit = _plan_cache.pop(key, None)
         if hit is not None:
-            if torch.equal(hit[0], uvw):
-                return key, hit
-            _retire(hit[1])
+            cached_uvw, plan, event = hit
+            torch.cuda.current_stream(uvw.device).wait_event(event)
+            if torch.equal(cached_uvw, uvw):
+                _mark_used(plan.workspace)
+                return key, (cached_uvw, plan)
+            _retire(plan, event)
     return key, (uvw, _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision,
                                 shift))
 
 
 def _checkin_plan(key, entry):
+    """Hand a plan back once the current stream has queued all its work."""
+    uvw, plan = entry
+    event = _done_event(uvw.device)
     if not _cache_on():
-        _retire(entry[1])
+        _retire(plan, event)
         return
     with _plan_lock:
         old = list(_plan_cache.values())
         _plan_cache.clear()
-        _plan_cache[key] = entry
-    for _, plan in old:
-        _retire(plan)
+        _plan_cache[key] = (uvw, plan, event)
+    for _, p, ev in old:
+        _retire(p, ev)
 
 
 def clear_plan_cache(release_memory=False):
@@ -163,8 +195,8 @@ def clear_plan_cache(release_memory=False):
     with _plan_lock:
         old = list(_plan_cache.values())
         _plan_cache.clear()
-    for _, plan in old:
-        _retire(plan)
+    for _, plan, ev in old:
+        _retire(plan, ev)
     if release_memory:
         with _plan_lock:
             _spare_ws.clear()
@@ -232,6 +264,29 @@ def predict_ng(bvis, model, **kwargs):
 
 def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
     """Invert visibilities to (image, sumwt) (``ng.py:136-282``)."""
+    return _invert(bvis, model, dopsf, normalise, None, kwargs)
+
+
+def residual_ng(bvis, model, normalise=True, **kwargs):
+    """Residual image and sumwt of ``bvis`` against ``model``: what RASCIL's
+    residual workflow computes as ``invert_ng(vis - predict_ng(zeroed copy
+    of vis, model), model)`` (``imaging_rsexecute.py:160-181``, with
+    ``zero_list`` / ``subtract_list`` ``:844-892``), done in one pass on the
+    GPU: the visibilities are uploaded once, each channel group's plan is
+    shared by the predict and the invert, and the model visibilities and
+    their difference never leave the device.  The model is also the image
+    template, as in the workflow."""
+    if numpy.isnan(numpy.asarray(bvis.uvw.data)).any():
+        # predict_ng and invert_ng treat non-finite uvw differently; compose them
+        pred = predict_ng(bvis, model, **kwargs)
+        return invert_ng(copy_visibility(bvis, vis=bvis["vis"].data - pred["vis"].data), model,
+                         normalise=normalise, **kwargs)
+    return _invert(bvis, model, False, normalise, model, kwargs)
+
+
+def _invert(bvis, model, dopsf, normalise, residual_of, kwargs):
+    """invert_ng, or with ``residual_of`` (a model image) the invert of
+    vis minus that model's prediction."""
     assert image_is_canonical(model)
     im = model
     epsilon = get_parameter(kwargs, "epsilon", 1e-12)
@@ -244,24 +299,29 @@ def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
     # shift_vis_to_image of ng.py:169-170, fused into the plan: the gridder
     # multiplies by the phase factor, so the visibilities are not copied
     _, shift = fused_phase_shift(bvis, im)
-    sbvis = bvis
-    freq = numpy.asarray(sbvis.frequency.data, dtype=numpy.float64)
-    nrows, nbaselines, vnchan, vnpol = sbvis.vis.shape
+    freq = numpy.asarray(bvis.frequency.data, dtype=numpy.float64)
+    nrows, nbaselines, vnchan, vnpol = bvis.vis.shape
     nchan, npol, ny, nx = im["pixels"].data.shape
     pixsize = abs(numpy.radians(im.image_acc.wcs.wcs.cdelt[0]))
     polmat = conversion_matrix(bvis.blockvisibility_acc.polarisation_frame,
                                im.image_acc.polarisation_frame)
     pm = None if (npol == vnpol and numpy.array_equal(polmat, numpy.eye(vnpol))) else polmat
+    pred_pm = None
+    if residual_of is not None:
+        assert npol == vnpol
+        pmat = conversion_matrix(im.image_acc.polarisation_frame,
+                                 bvis.blockvisibility_acc.polarisation_frame)
+        pred_pm = None if numpy.array_equal(pmat, numpy.eye(vnpol)) else pmat
     vis_to_im = _vis_to_im(model, freq)
     R = nrows * nbaselines
-    uvw = _device_uvw(sbvis.uvw.data, device)
+    uvw = _device_uvw(bvis.uvw.data, device)
     vis = None
     if not dopsf:
-        vis = _to_device(sbvis["vis"].data.reshape(R, vnchan, vnpol), cdt, device)
-    flags = _to_device(sbvis["flags"].data.reshape(R, vnchan, vnpol), None, device)
+        vis = _to_device(bvis["vis"].data.reshape(R, vnchan, vnpol), cdt, device)
+    flags = _to_device(bvis["flags"].data.reshape(R, vnchan, vnpol), None, device)
     if flags.dtype != torch.int64:
         flags = (flags != 0).to(torch.uint8)
-    wgt = _to_device(sbvis["imaging_weight"].data.reshape(R, vnchan, vnpol), rdt, device)
+    wgt = _to_device(bvis["imaging_weight"].data.reshape(R, vnchan, vnpol), rdt, device)
 
     pdt = model["pixels"].data.dtype
     acc = torch.zeros((nchan, npol, ny, nx), dtype=torch.float64, device=device)
@@ -282,7 +342,11 @@ def invert_ng(bvis, model, dopsf=False, normalise=True, **kwargs):
         key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol,
                                     precision, shift)
         try:
-            dirty, sw = entry[1].ms2dirty(pick(vis), wgt=pick(wgt), flags=pick(flags),
+            gvis = pick(vis)
+            if residual_of is not None:
+                img = _to_device(residual_of["pixels"].data[ichan], rdt, device)
+                gvis = gvis - entry[1].dirty2ms(img, polmat=pred_pm, npol_vis=vnpol, layout="yx")
+            dirty, sw = entry[1].ms2dirty(gvis, wgt=pick(wgt), flags=pick(flags),
                                           polmat=pm, psf=dopsf, layout="yx", sumwt=True)
             acc[ichan] += dirty
             sw = sw.cpu().numpy()
