@@ -75,6 +75,12 @@ def parse():
                     help="per-plane transforms of the FP32 form (auto: column kernels where "
                          "they apply)")
     ap.add_argument("--json-out", default=None)
+    ap.add_argument("--path", default="imaging",
+                    choices=["imaging", "weights", "rotation", "lists"],
+                    help="imaging: the headline invert+predict step (default); weights: "
+                         "imaging weights; rotation: the phase rotation (standalone kernel and "
+                         "its cost fused into the imaging step); lists: the list workflows on "
+                         "256 uneven snapshots")
     return ap.parse_args()
 
 
@@ -423,6 +429,359 @@ def e2e_run(wl, steps):
                    "host BlockVisibility (page-locked arrays) / Image"}
 
 
+# ---------------------------------------------------------------------------
+# the paths either side of the imaging step (--path): each prints its own line
+
+def _ptr(t):
+    import ctypes
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _event_loop(fn, steps, warmup, sampler=None, profile=True):
+    """ms per call of fn() timed with CUDA events on the current stream
+    (after warm-up), with the per-kernel profile of the timed calls."""
+    import torch
+    from rascil_gb300 import _lib
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    if profile:
+        _lib.profile_reset()
+        _lib.profile_enable(True)
+    if sampler:
+        sampler.start()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    stats = None
+    if profile:
+        _lib.profile_enable(False)
+        stats = _lib.profile_read()
+    return a.elapsed_time(b) / steps, clocks, stats
+
+
+def _aux_line(args, metric, value, unit, ms, workload, roof, kernels, clocks, launches, **extra):
+    line = {"path": args.path, "metric": metric, "value": round(value, 3), "unit": unit,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "data": "synthetic (seeded)", "config": workload, "clocks": clocks,
+            "roofline": roof, "gpu_launches": launches, "kernels": kernels}
+    line.update(extra)
+    return line
+
+
+def bench_weights(args):
+    """weight_visibility (uniform, the reference's default) over every
+    sample of the workload: gb_weight_visibility on device-resident arrays,
+    then end to end on a host BlockVisibility."""
+    import torch
+    from rascil_gb300 import _lib
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.data_models import BlockVisibility
+    from rascil_gb300.imaging import weight_visibility
+    from rascil_gb300.polarisation import PolarisationFrame
+    device = torch.device("cuda", torch.cuda.current_device())
+    lib = _lib.load()
+    ov = SCALES[args.scale]
+    uvw, freq, pc, cfg = sim.observation(args.config, seed=0, ntimes=ov["ntimes"],
+                                         nchan=ov["nchan"], npixel=ov["npixel"])
+    nt, nbl, _ = uvw.shape
+    R, C, P = nt * nbl, len(freq), PolarisationFrame(cfg["pol"]).npol
+    npix, cell = cfg["npixel"], cfg["cellsize"]
+    nvis = R * C * P
+    g = torch.Generator(device=device)
+    g.manual_seed(7)
+    uvw_d = torch.from_numpy(uvw.reshape(-1, 3).copy()).to(device)
+    freq_d = torch.from_numpy(freq.copy()).to(device)
+    weight = torch.rand((R, C, P), generator=g, device=device, dtype=torch.float64).add_(0.5)
+    imw = torch.rand((R, C, P), generator=g, device=device, dtype=torch.float64)
+    imw.mul_(0.4).add_(0.8).mul_(weight)
+    flags = (torch.rand((R, C, P), generator=g, device=device) < 0.05).to(torch.int64)
+    v2i = torch.zeros(C, dtype=torch.int32, device=device)  # MFS image: one channel
+    grid = torch.empty((1, npix, npix, P), dtype=torch.float64, device=device)
+    cells = torch.empty((R, C), dtype=torch.int32, device=device)
+    out = torch.empty_like(weight)
+    sums = torch.empty(2, dtype=torch.float64, device=device)
+    cdx, cdy = -numpy.degrees(cell), numpy.degrees(cell)
+    stream = torch.cuda.current_stream(device)
+
+    def call(scheme, robustness=0.0):
+        _lib.check(lib.gb_weight_visibility(
+            _ptr(uvw_d), _ptr(freq_d), R, C, P, _ptr(v2i), 1, npix, npix, cdx, cdy, _ptr(weight),
+            _ptr(imw), _ptr(flags), _lib.GB_FLAGS_I64, scheme, robustness, _ptr(grid),
+            _ptr(cells), _ptr(out), _ptr(sums), _ptr_stream(stream)), "gb_weight_visibility")
+
+    sampler = ClockSampler(device.index)
+    ms, clocks, stats = _event_loop(lambda: call(_lib.GB_WEIGHT_UNIFORM), args.steps,
+                                    args.warmup, sampler)
+    roof, kernels = roofline(stats, load_peaks())
+    launches = sum(v["launches"] for v in stats.values()) // args.steps
+    others = {}
+    for name, scheme, rob in (("natural", _lib.GB_WEIGHT_NATURAL, 0.0),
+                              ("robust_0", _lib.GB_WEIGHT_ROBUST, 0.0)):
+        m, _, _ = _event_loop(lambda: call(scheme, rob), args.steps, 1, profile=False)
+        others[name] = {"ms": round(m, 3), "value": round(nvis / (m * 1e-3) / 1e6, 1)}
+    # CPU baseline: the oracle (numpy, the reference's own algorithm) on the
+    # first 1/64 of the rows
+    from oracle import weighting as ow
+    rs = max(1, R // 64)
+    sl = slice(0, rs)
+    hw = weight[sl].cpu().numpy()
+    him = imw[sl].cpu().numpy()
+    hf = flags[sl].cpu().numpy()
+    t0 = time.perf_counter()
+    ow.weight_visibility(uvw.reshape(-1, 3)[sl], freq, hw, him, hf, numpy.zeros(C, int), 1, npix,
+                         npix, cdx, cdy, "uniform")
+    cpu_dt = time.perf_counter() - t0
+    cpu = {"value": round(rs * C * P / cpu_dt / 1e6, 3), "unit": "Mvis/s", "cores": 1,
+           "kind": "port", "sample": "oracle/weighting.py (numpy, uniform) on the first %d of %d "
+           "rows (%d samples): %.1f s" % (rs, R, rs * C * P, cpu_dt)}
+    del hw, him, hf
+    # end to end: weight_visibility on a host BlockVisibility (page-locked arrays)
+    def pinned_from(t):
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t)
+        return h.numpy()
+
+    shape = (nt, nbl, C, P)
+    bvis = BlockVisibility(torch.empty(shape, dtype=torch.complex64, pin_memory=True).numpy(),
+                           pinned_from(uvw_d).reshape(nt, nbl, 3), freq, pc,
+                           PolarisationFrame(cfg["pol"]),
+                           flags=pinned_from(flags).reshape(shape),
+                           weight=pinned_from(weight).reshape(shape),
+                           imaging_weight=pinned_from(imw).reshape(shape))
+    model = sim.model_image(cfg, ([], [], [], [], []), pc, freq)
+    del weight, imw, flags, out, grid, cells
+    torch.cuda.empty_cache()
+    weight_visibility(bvis, model, weighting="uniform")  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        weight_visibility(bvis, model, weighting="uniform")
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.e2e_steps
+    e2e = {"value": round(nvis / dt / 1e6, 3), "unit": "Mvis/s",
+           "h2d_bytes_per_step": int(3 * 8 * nvis + 24 * R),
+           "d2h_bytes_per_step": int(8 * nvis), "s_per_step": round(dt, 3),
+           "api": "rascil_gb300.imaging.weight_visibility(bvis, model, 'uniform') on page-locked "
+                  "host arrays (weight, imaging_weight, int64 flags, uvw)"}
+    workload = {"workload": "imaging weights (uniform) of %s %s: %d rows x %d chan x %d pol "
+                            "onto the %d^2 MFS uv grid (cell %g rad)"
+                            % (args.config, args.scale, R, C, P, npix, cell),
+                "nvis": nvis, "l2": "inputs larger than L2 (%.1f GB f64 weights and flags)"
+                                    % (3 * 8 * nvis / 1e9)}
+    return _aux_line(args, "Mvis/s imaging weights (weight_visibility, uniform) on 1 GB300",
+                     nvis / (ms * 1e-3) / 1e6, "Mvis/s", ms, workload, roof, kernels, clocks,
+                     launches, dtype="f64", schemes=others, cpu_baseline=cpu, e2e=e2e)
+
+
+def bench_rotation(args):
+    """The phase rotation: gb_phase_rotate over the workload's complex64
+    visibilities in place, and the imaging step with an image centred 0.01
+    rad away from the phase centre (rotation fused into the plan) against
+    the centred step."""
+    import torch
+    from rascil_gb300 import _lib
+    from rascil_gb300.data_models import BlockVisibility, SkyDirection
+    from rascil_gb300.imaging.base import phaserotate_visibility, phasor_direction
+    from rascil_gb300.polarisation import PolarisationFrame
+    from rascil_gb300.wgridder import Plan
+    device = torch.device("cuda", torch.cuda.current_device())
+    lib = _lib.load()
+    wl = Workload(args.config, args.scale, device)
+    new = SkyDirection(wl.phasecentre.ra.rad + 0.01, wl.phasecentre.dec.rad - 0.005)
+    s = phasor_direction(new, wl.phasecentre)
+    stream = torch.cuda.current_stream(device)
+    vis = wl.vis32.clone()
+    flip = [0]
+
+    def call():
+        flip[0] ^= 1  # forward, then inverse: the data stay bounded
+        _lib.check(lib.gb_phase_rotate(_ptr(wl.uvw_raw), _ptr(wl.freq_dev), wl.nrows, wl.nchan,
+                                       wl.npv, _ptr(vis), _lib.GB_FP32, s[0], s[1], s[2], flip[0],
+                                       _ptr_stream(stream)), "gb_phase_rotate")
+
+    sampler = ClockSampler(device.index)
+    ms, clocks, stats = _event_loop(call, args.steps, args.warmup, sampler)
+    roof, kernels = roofline(stats, load_peaks())
+    del vis
+    torch.cuda.empty_cache()
+
+    # fused: the imaging step with and without the shift (plan-frame coefficients)
+    def imaging_step(shift):
+        plan = Plan(wl.uvw, wl.freq_dev, wl.npixel, wl.npixel, wl.cell, wl.cell, wl.epsilon,
+                    True, npol=wl.npol, precision="fp32", phase_shift=shift)
+        plan.ms2dirty(wl.vis32, wgt=wl.wgt32, polmat=wl.pm_in, layout="yx")
+        plan.dirty2ms(wl.model32, polmat=wl.pm_out, npol_vis=wl.npv, layout="yx")
+        plan.close()
+
+    fused = {}
+    for name, shift in (("centred", (0.0, 0.0, 0.0)), ("offset", (-s[0], s[1], -s[2]))):
+        m, _, _ = _event_loop(lambda: imaging_step(shift), 2, 1, profile=False)
+        fused[name + "_ms"] = round(m, 1)
+    fused["note"] = ("plan + invert + predict of the whole workload; 'offset' images 0.01 rad "
+                     "from the phase centre with the rotation fused into the item factors")
+    # CPU baseline: the oracle rotation (numpy) on the first 1/64 of the rows
+    from oracle import rotation as orot
+    rs = max(1, wl.nrows // 64)
+    hv = wl.vis32[:rs].cpu().numpy()
+    t0 = time.perf_counter()
+    orot.phaserotate(hv, wl.uvw_host.reshape(-1, 3)[:rs], wl.freq, (s[0], s[1], s[2]))
+    cpu_dt = time.perf_counter() - t0
+    cpu = {"value": round(rs * wl.nchan * wl.npv / cpu_dt / 1e6, 3), "unit": "Mvis/s",
+           "cores": 1, "kind": "port",
+           "sample": "oracle/rotation.py (numpy) on the first %d of %d rows: %.1f s"
+                     % (rs, wl.nrows, cpu_dt)}
+    # end to end: phaserotate_visibility on a host BlockVisibility (page-locked vis)
+    shape = (wl.ntimes, wl.nbl, wl.nchan, wl.npv)
+    hvis = torch.empty(shape, dtype=torch.complex64, pin_memory=True)
+    hvis.copy_(wl.vis32.reshape(shape))
+    bvis = BlockVisibility(hvis.numpy(), wl.uvw_host, wl.freq, wl.phasecentre,
+                           PolarisationFrame(wl.cfg["pol"]))
+    phaserotate_visibility(bvis, new)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        phaserotate_visibility(bvis, new)
+    dt = (time.perf_counter() - t0) / args.e2e_steps
+    e2e = {"value": round(wl.nvis / dt / 1e6, 3), "unit": "Mvis/s",
+           "h2d_bytes_per_step": int(8 * wl.nvis + 24 * wl.nrows),
+           "d2h_bytes_per_step": int(8 * wl.nvis), "s_per_step": round(dt, 3),
+           "api": "rascil_gb300.imaging.base.phaserotate_visibility on a host BlockVisibility "
+                  "(includes the reference's deep copy of the other arrays)"}
+    workload = dict(workload_config(wl))
+    workload["workload"] = "phase rotation of " + workload["workload"]
+    return _aux_line(args, "Mvis/s phase rotation (gb_phase_rotate, complex64 in place) on 1 "
+                     "GB300", wl.nvis / (ms * 1e-3) / 1e6, "Mvis/s", ms, workload, roof, kernels,
+                     clocks, 1, dtype="f32", fused_in_imaging=fused, cpu_baseline=cpu, e2e=e2e)
+
+
+def bench_lists(args):
+    """invert_list / residual_list over 256 uneven snapshots (config 3:
+    32-512 antennas, 1-8 channels, 1-16 times, 256-2048 pixel images),
+    page-locked host BlockVisibility per snapshot, FP32 form at eps 1e-5.
+    Timed with the host clock: every call ends with its results on the host."""
+    import torch
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.data_models import BlockVisibility, SkyDirection, create_image
+    from rascil_gb300.imaging.ng import clear_plan_cache
+    from rascil_gb300.polarisation import PolarisationFrame
+    from rascil_gb300 import workflows as wf
+    snaps = sim.snapshot_batch(256)
+    rng = numpy.random.default_rng(3)
+    pc = SkyDirection(0.0, numpy.radians(-45.0))
+    blocks, models = [], []
+    for sn in snaps:
+        nt, nbl, _ = sn["uvw"].shape
+        shape = (nt, nbl, len(sn["freq"]), 1)
+        vis = torch.empty(shape, dtype=torch.complex64, pin_memory=True).numpy()
+        vis[...] = (rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(numpy.complex64)
+        blocks.append(BlockVisibility(vis, sn["uvw"], sn["freq"], pc, PolarisationFrame("stokesI")))
+        bw = sn["freq"].max() - sn["freq"].min() + 1.0
+        models.append(create_image(sn["npix"], sn["cell"], pc, frequency=[sn["freq"].mean()],
+                                   channel_bandwidth=[bw]))
+    nvis = sum(sn["nvis"] for sn in snaps)
+    kw = dict(epsilon=1e-5, precision="fp32")
+
+    def timed(fn):
+        clear_plan_cache(release_memory=True)
+        torch.cuda.empty_cache()
+        fn()  # warm-up
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return float(numpy.median(ts))
+
+    res = {}
+    for streams in (1, 4, 8):
+        dt = timed(lambda: wf.invert_list_rsexecute_workflow(blocks, models, "ng",
+                                                             streams=streams, **kw))
+        res["invert_list_streams_%d" % streams] = {"s": round(dt, 3),
+                                                   "value": round(nvis / dt / 1e6, 2)}
+    dt_res = timed(lambda: wf.residual_list_rsexecute_workflow(blocks, models, "ng", streams=4,
+                                                               **kw))
+
+    def composed():
+        mv = wf.predict_list_rsexecute_workflow(wf.zero_list_rsexecute_workflow(blocks), models,
+                                                "ng", streams=4, **kw)
+        return wf.invert_list_rsexecute_workflow(wf.subtract_list_rsexecute_workflow(blocks, mv),
+                                                 models, "ng", streams=4, **kw)
+
+    dt_comp = timed(composed)
+    res["residual_list_fused_streams_4"] = {"s": round(dt_res, 3),
+                                            "value": round(2 * nvis / dt_res / 1e6, 2)}
+    res["residual_list_composed_streams_4"] = {"s": round(dt_comp, 3),
+                                               "value": round(2 * nvis / dt_comp / 1e6, 2)}
+    # device time of one sequential pass, per kernel: how much of the list's
+    # wall time the GPU is busy
+    from rascil_gb300 import _lib
+    clear_plan_cache(release_memory=True)
+    _lib.profile_reset()
+    _lib.profile_enable(True)
+    t0 = time.perf_counter()
+    wf.invert_list_rsexecute_workflow(blocks, models, "ng", streams=1, **kw)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    _lib.profile_enable(False)
+    stats = _lib.profile_read()
+    busy = sum(v["ms"] for v in stats.values()) / 1e3
+    top = sorted(stats.items(), key=lambda kv: -kv[1]["ms"])[:6]
+    res["device_profile_streams_1"] = {
+        "wall_s": round(wall, 3), "kernel_s": round(busy, 3),
+        "top": {k: {"ms": round(v["ms"], 1), "launches": v["launches"]} for k, v in top}}
+    clear_plan_cache(release_memory=True)
+    best = max((v["value"], k) for k, v in res.items() if k.startswith("invert_list"))
+    # CPU baseline: the oracle's C gridder (ms2dirty, FP64, all cores) over
+    # the first snapshots until ~10 s of work
+    from oracle import cgridder
+    done, t_cpu = 0, 0.0
+    for sn, b in zip(snaps, blocks):
+        if t_cpu > 10.0:
+            break
+        u = sn["uvw"].reshape(-1, 3).copy()
+        u[:, 0] *= -1.0
+        u[:, 2] *= -1.0
+        ms_ = b["vis"].data.reshape(u.shape[0], -1).astype(numpy.complex128)
+        t0 = time.perf_counter()
+        cgridder.ms2dirty(u, sn["freq"], ms_, None, sn["npix"], sn["npix"], sn["cell"],
+                          sn["cell"], 1e-5, True)
+        t_cpu += time.perf_counter() - t0
+        done += sn["nvis"]
+    cpu = {"value": round(done / t_cpu / 1e6, 3), "unit": "Mvis/s",
+           "cores": cgridder.max_threads(), "kind": "port",
+           "sample": "oracle C gridder ms2dirty (FP64, OpenMP) on the first %d vis of the list: "
+                     "%.1f s" % (done, t_cpu)}
+    workload = {"workload": "invert_list over 256 snapshots (32-512 antennas in 1 km, 1-8 chan "
+                            "in 100-200 MHz, 1-16 times, 256-2048 px, cell 1/(2.2 max|uv|)), "
+                            "eps 1e-5, FP32 form, Stokes I, page-locked host arrays",
+                "nvis": int(nvis), "snapshots": len(snaps)}
+    t_best = res[best[1]]["s"]
+    return _aux_line(args, "Mvis/s invert_list over 256 uneven snapshots on 1 GB300 (host data)",
+                     best[0], "Mvis/s", t_best * 1e3, workload, None, None, None, None,
+                     dtype="f32", best=best[1], runs=res, cpu_baseline=cpu,
+                     e2e={"value": best[0], "unit": "Mvis/s",
+                          "h2d_bytes_per_step": int(8 * nvis + 24 * sum(
+                              sn["uvw"].shape[0] * sn["uvw"].shape[1] for sn in snaps)),
+                          "d2h_bytes_per_step": int(sum(8 * sn["npix"] ** 2 for sn in snaps))},
+                     timing="host clock around each whole list call (results on the host)")
+
+
+def _ptr_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+AUX_PATHS = {"weights": bench_weights, "rotation": bench_rotation, "lists": bench_lists}
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -496,6 +855,13 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.path != "imaging":
+        line = AUX_PATHS[args.path](args)
+        print(json.dumps(line))
+        if args.json_out:
+            with open(args.json_out, "w") as f:
+                json.dump(line, f, indent=1)
         return
     import torch
     GRID_BUDGET[0] = int(args.grid_budget_gb * (1 << 30))

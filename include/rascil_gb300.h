@@ -289,7 +289,8 @@ int gb_wrange_noalloc(const double *uvw_dev, const double *freq_dev, int64_t nro
  *   weight_dev, imaging_weight_dev  [nrows][nchan][npol] f64
  *   flags_dev     [nrows][nchan][npol] of flags_type, or NULL (GB_FLAGS_NONE)
  *   cdelt_x_deg, cdelt_y_deg  the image WCS's cdelt[0], cdelt[1] (degrees)
- *   grid_dev      [nchan_img][npol][ny][nx] f64 scratch: the gridded weights on return
+ *   grid_dev      [nchan_img][ny][nx][npol] f64 scratch: the gridded weights on return
+ *   cells_dev     [nrows][nchan] u32 scratch: each sample's cell v * nx + u
  *   imaging_weight_out_dev  [nrows][nchan][npol] f64 (may alias neither input)
  *   sums_dev      [2] f64: sum(G), sum(G^2) on return
  * Synchronises `stream` (to report) and returns GB_ERR_OUT_OF_GRID when a
@@ -301,8 +302,8 @@ int gb_weight_visibility(const double *uvw_dev, const double *freq_dev, int64_t 
                          double cdelt_y_deg, const double *weight_dev,
                          const double *imaging_weight_dev, const void *flags_dev,
                          int32_t flags_type, int32_t weighting, double robustness,
-                         double *grid_dev, double *imaging_weight_out_dev, double *sums_dev,
-                         void *stream);
+                         double *grid_dev, uint32_t *cells_dev,
+                         double *imaging_weight_out_dev, double *sums_dev, void *stream);
 
 /* Tangent-plane phase rotation of visibilities in place, RASCIL's
  * phaserotate_visibility(tangent=True) (visibility/base.py:296-357) with

@@ -31,6 +31,10 @@ enum ProfId {
   kProfRowsInv,
   kProfRowsFwd,
   kProfGridZero,
+  kProfWeightGrid,
+  kProfWeightSums,
+  kProfWeightApply,
+  kProfRotate,
   kProfCount
 };
 

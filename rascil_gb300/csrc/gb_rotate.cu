@@ -74,6 +74,8 @@ extern "C" int gb_phase_rotate(const double *uvw_dev, const double *freq_dev, in
       (unsigned)std::min<int64_t>((n + kThreads - 1) / kThreads, (int64_t)nsm * 16);
   // forward: the reference multiplies by conj(phasor) = exp(+2 pi i d)
   const double sign = inverse ? -1.0 : 1.0;
+  const double cb = precision == GB_FP64 ? 16.0 : 8.0;
+  ProfScope ps(kProfRotate, s, 2.0 * cb * (double)n * npol + 24.0 * nrows);
   if (precision == GB_FP64)
     k_rotate<double><<<blocks, kThreads, 0, s>>>(uvw_dev, freq_dev, nrows, nchan, npol, s_l,
                                                  s_m, s_n, sign,

@@ -3,18 +3,23 @@
 //
 //   k_wgrid    every (row, channel): its cell on the image-sized uv grid
 //              (griddata/operations.py:71-107 builds the grid's WCS,
-//              griddata/gridding.py:68-175 maps u, v to the nearest cell);
-//              the flagged imaging weights of its pols are added to the grid
-//              with FP64 atomics (gridding.py:260-306);
+//              griddata/gridding.py:68-175 maps u, v to the nearest cell),
+//              stored for k_wapply; the flagged imaging weights of its pols
+//              are added to the grid with FP64 atomics (gridding.py:260-306);
 //   k_wsums    sum(G) and sum(G^2) over the grid (the robust factor:
 //              sum(G) equals the sum of all flagged imaging weights);
-//   k_wapply   the new imaging weight of every sample (gridding.py:332-425).
+//   k_wapply   the new imaging weight of every sample (gridding.py:332-425)
+//              from its stored cell.
+//
+// The grid is [image channel][v][u][pol]: the pols of a cell share one
+// 32-byte sector, so a sample's atomics and its gather touch one sector.
 //
 // The cell is computed in FP64 with every rounding step explicit, in the
 // order ((u - 0) / cdelt_u + crpix) - 1 then round-half-to-even, so it is
 // bit-identical to the CPU restatement (and to the reference's linear WCS).
 #include <cfloat>
 #include <cmath>
+#include <vector>
 
 #include "gb_plan.cuh"
 
@@ -35,11 +40,9 @@ __device__ __forceinline__ double nan_to_num(double x) {
   return x;
 }
 
-// Cell (pu, pv) of row r, channel c; false if it lies outside the grid.
+// Cell (pu, pv) of row r at k = f / c; false if it lies outside the grid.
 __device__ __forceinline__ bool weight_cell(const WeightGeom &w, const double *__restrict__ uvw,
-                                            const double *__restrict__ freq, int64_t r, int c,
-                                            int &pu, int &pv) {
-  const double k = gb_div(freq[c], kSpeedOfLight);
+                                            double k, int64_t r, int &pu, int &pv) {
   const double u = nan_to_num(gb_mul(uvw[3 * r], k));
   const double v = nan_to_num(gb_mul(uvw[3 * r + 1], k));
   const double xu = rint(gb_sub(gb_add(gb_div(u, w.cdu), w.crpu), 1.0));
@@ -56,25 +59,52 @@ __device__ __forceinline__ double flag_factor(const void *flags, int ftype, int6
   return 1.0;
 }
 
+constexpr uint32_t kNoCell = 0xffffffffu;
+// channels whose f / c k_wgrid tabulates in shared memory (else per sample)
+constexpr int kMaxTableChan = 4096;
+
+// 1 / g for g > 0 by Newton-Raphson (r <- r + r (1 - g r), twice) from the
+// FP32 reciprocal: the relative error squares each step, 2^-23 -> 2^-46 ->
+// below FP64 rounding, in four FMAs instead of an IEEE FP64 division (FP64
+// runs at 1/64 of the FP32 rate on this part).  g outside FP32's normal
+// range takes the division.
+__device__ __forceinline__ double recip_pos(double g) {
+  const float gf = (float)g;
+  if (!(gf >= FLT_MIN && gf <= 0.5f * FLT_MAX)) return 1.0 / g;
+  double r = (double)__frcp_rn(gf);
+  r = fma(r, fma(-g, r, 1.0), r);
+  r = fma(r, fma(-g, r, 1.0), r);
+  return r;
+}
+
 __global__ void k_wgrid(const WeightGeom w, const double *__restrict__ uvw,
                         const double *__restrict__ freq, const double *__restrict__ imw,
                         const void *__restrict__ flags, double *__restrict__ grid,
-                        uint32_t *__restrict__ status) {
+                        uint32_t *__restrict__ cells, uint32_t *__restrict__ status) {
+  extern __shared__ double s_k[];  // f / c per channel (C <= kMaxTableChan)
+  const bool table = w.C <= kMaxTableChan;
+  if (table) {
+    for (int c = threadIdx.x; c < w.C; c += blockDim.x) s_k[c] = gb_div(freq[c], kSpeedOfLight);
+    __syncthreads();
+  }
   const int64_t n = w.R * w.C;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = i / w.C;
     const int c = (int)(i - r * w.C);
+    const double k = table ? s_k[c] : gb_div(freq[c], kSpeedOfLight);
     int pu, pv;
-    if (!weight_cell(w, uvw, freq, r, c, pu, pv)) {
+    if (!weight_cell(w, uvw, k, r, pu, pv)) {
+      cells[i] = kNoCell;
       atomicOr(status, 1u);
       continue;
     }
-    const int ic = w.vis_to_im[c];
+    const uint32_t cell = (uint32_t)pv * (uint32_t)w.nx + (uint32_t)pu;
+    cells[i] = cell;
+    double *g = grid + ((int64_t)w.vis_to_im[c] * w.ny * w.nx + cell) * w.P;
     for (int p = 0; p < w.P; ++p) {
       const int64_t j = i * w.P + p;
-      const double fw = imw[j] * flag_factor(flags, w.ftype, j);
-      atomicAdd(&grid[(((int64_t)ic * w.P + p) * w.ny + pv) * w.nx + pu], fw);
+      atomicAdd(&g[p], imw[j] * flag_factor(flags, w.ftype, j));
     }
   }
 }
@@ -109,11 +139,11 @@ __global__ void k_wsums(const double *__restrict__ grid, int64_t n, double *__re
   }
 }
 
-__global__ void k_wapply(const WeightGeom w, const double *__restrict__ uvw,
-                         const double *__restrict__ freq, const double *__restrict__ imw,
-                         const double *__restrict__ wgt, const void *__restrict__ flags,
-                         const double *__restrict__ grid, const double *__restrict__ sums,
-                         int scheme, double a2, double *__restrict__ out) {
+__global__ void k_wapply(const WeightGeom w, const uint32_t *__restrict__ cells,
+                         const double *__restrict__ imw, const double *__restrict__ wgt,
+                         const void *__restrict__ flags, const double *__restrict__ grid,
+                         const double *__restrict__ sums, int scheme, double a2,
+                         double *__restrict__ out) {
   const int64_t n = w.R * w.C;
   // robust: f2 = (5 10^-R)^2 sum(w) / sum(G^2), with a2 = (5 10^-R)^2 from the host
   const double f2 = scheme == GB_WEIGHT_ROBUST ? a2 * sums[0] / sums[1] : 0.0;
@@ -123,18 +153,18 @@ __global__ void k_wapply(const WeightGeom w, const double *__restrict__ uvw,
       for (int p = 0; p < w.P; ++p) out[i * w.P + p] = wgt[i * w.P + p];
       continue;
     }
-    const int64_t r = i / w.C;
-    const int c = (int)(i - r * w.C);
-    int pu = 0, pv = 0;
-    const bool in = weight_cell(w, uvw, freq, r, c, pu, pv);  // out-of-grid already reported
-    const int ic = w.vis_to_im[c];
+    const int c = (int)(i % w.C);
+    const uint32_t cell = cells[i];  // kNoCell: off the grid, already reported
+    const double *gp =
+        grid + (cell != kNoCell ? ((int64_t)w.vis_to_im[c] * w.ny * w.nx + cell) * w.P : 0);
     for (int p = 0; p < w.P; ++p) {
       const int64_t j = i * w.P + p;
       const double x = imw[j] * flag_factor(flags, w.ftype, j);
-      const double g = in ? grid[(((int64_t)ic * w.P + p) * w.ny + pv) * w.nx + pu] : 0.0;
+      const double g = cell != kNoCell ? gp[p] : 0.0;
       double y = 0.0;
       if (g > 0.0) {
-        y = scheme == GB_WEIGHT_UNIFORM ? x * (x / g) : x * ((1.0 + f2 * x) / (1.0 + f2 * g));
+        y = scheme == GB_WEIGHT_UNIFORM ? x * (x * recip_pos(g))
+                                        : x * ((1.0 + f2 * x) * recip_pos(1.0 + f2 * g));
       }
       out[j] = y;
     }
@@ -151,15 +181,16 @@ extern "C" int gb_weight_visibility(const double *uvw_dev, const double *freq_de
                                     double cdelt_x_deg, double cdelt_y_deg,
                                     const double *weight_dev, const double *imaging_weight_dev,
                                     const void *flags_dev, int32_t flags_type, int32_t weighting,
-                                    double robustness, double *grid_dev,
+                                    double robustness, double *grid_dev, uint32_t *cells_dev,
                                     double *imaging_weight_out_dev, double *sums_dev,
                                     void *stream) {
   if (!uvw_dev || !freq_dev || !vis_to_im_dev || !weight_dev || !imaging_weight_dev ||
-      !grid_dev || !imaging_weight_out_dev || !sums_dev) {
+      !grid_dev || !cells_dev || !imaging_weight_out_dev || !sums_dev) {
     set_error("gb_weight_visibility: NULL argument");
     return GB_ERR_INVALID_ARG;
   }
   if (nrows <= 0 || nchan <= 0 || npol <= 0 || nchan_img <= 0 || nx <= 0 || ny <= 0 ||
+      (int64_t)nx * ny >= (int64_t)kNoCell ||
       !(cdelt_x_deg != 0.0) || !(cdelt_y_deg != 0.0)) {
     set_error("gb_weight_visibility: empty or invalid geometry");
     return GB_ERR_INVALID_ARG;
@@ -178,6 +209,21 @@ extern "C" int gb_weight_visibility(const double *uvw_dev, const double *freq_de
     return GB_ERR_INVALID_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  // every channel must map to an image channel: the kernels index the grid
+  // with it (the reference's numpy indexing raises for the same input)
+  {
+    std::vector<int32_t> v2i((size_t)nchan);
+    GB_CUDA(cudaMemcpyAsync(v2i.data(), vis_to_im_dev, sizeof(int32_t) * (size_t)nchan,
+                            cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    for (int32_t c = 0; c < nchan; ++c) {
+      if (v2i[c] < 0 || v2i[c] >= nchan_img) {
+        set_error("gb_weight_visibility: channel %d maps to image channel %d, outside [0, %d)",
+                  (int)c, (int)v2i[c], (int)nchan_img);
+        return GB_ERR_INVALID_ARG;
+      }
+    }
+  }
   const double d2r = M_PI / 180.0;
   WeightGeom w;
   w.R = nrows;
@@ -204,18 +250,36 @@ extern "C" int gb_weight_visibility(const double *uvw_dev, const double *freq_de
   const int64_t n = nrows * (int64_t)nchan;
   const unsigned blocks =
       (unsigned)std::min<int64_t>((n + kThreads - 1) / kThreads, (int64_t)nsm * 16);
-  k_wgrid<<<blocks, kThreads, 0, s>>>(w, uvw_dev, freq_dev, imaging_weight_dev, flags_dev,
-                                      grid_dev, status);
-  GB_LAUNCH_CHECK("k_wgrid");
+  // algorithmic bytes: per sample its imaging weight and flag (and weight /
+  // new weight in the apply), per row its uvw; the grid once per pass
+  const double fb = flags_type == GB_FLAGS_I64 ? 8.0 : (flags_type == GB_FLAGS_U8 ? 1.0 : 0.0);
+  const double ns = (double)n * npol;
+  {
+    ProfScope ps(kProfWeightGrid, s, ns * (8.0 + fb) + 4.0 * n + 24.0 * nrows + 8.0 * ngrid);
+    const size_t smem = nchan <= kMaxTableChan ? sizeof(double) * (size_t)nchan : 0;
+    k_wgrid<<<blocks, kThreads, smem, s>>>(w, uvw_dev, freq_dev, imaging_weight_dev, flags_dev,
+                                           grid_dev, cells_dev, status);
+    GB_LAUNCH_CHECK("k_wgrid");
+  }
   const unsigned gblocks =
       (unsigned)std::min<int64_t>((ngrid + kThreads - 1) / kThreads, (int64_t)nsm * 8);
-  k_wsums<<<gblocks, kThreads, 0, s>>>(grid_dev, ngrid, sums_dev);
-  GB_LAUNCH_CHECK("k_wsums");
+  {
+    ProfScope ps(kProfWeightSums, s, 8.0 * ngrid);
+    k_wsums<<<gblocks, kThreads, 0, s>>>(grid_dev, ngrid, sums_dev);
+    GB_LAUNCH_CHECK("k_wsums");
+  }
   const double a = 5.0 * std::pow(10.0, -robustness);
-  k_wapply<<<blocks, kThreads, 0, s>>>(w, uvw_dev, freq_dev, imaging_weight_dev, weight_dev,
-                                       flags_dev, grid_dev, sums_dev, weighting, a * a,
-                                       imaging_weight_out_dev);
-  GB_LAUNCH_CHECK("k_wapply");
+  {
+    // uniform / robust: imaging weight, flag, grid value in, new weight out;
+    // per (row, channel) its cell
+    const double per = weighting == GB_WEIGHT_NATURAL ? 16.0 : 24.0 + fb;
+    ProfScope ps(kProfWeightApply, s,
+                 ns * per + (weighting == GB_WEIGHT_NATURAL ? 0.0 : 4.0 * n));
+    k_wapply<<<blocks, kThreads, 0, s>>>(w, cells_dev, imaging_weight_dev, weight_dev, flags_dev,
+                                         grid_dev, sums_dev, weighting, a * a,
+                                         imaging_weight_out_dev);
+    GB_LAUNCH_CHECK("k_wapply");
+  }
   uint32_t hs = 0;
   GB_CUDA(cudaMemcpyAsync(&hs, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaFreeAsync(status, s));

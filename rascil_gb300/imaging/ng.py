@@ -23,7 +23,8 @@ Same signatures, keyword arguments, defaults and results as
   into page-locked arrays (torch's host caching allocator).
 
 Extra keyword arguments: ``precision`` ("fp64", the default, matches
-the reference's complex128 path; "fp32" is the fast form), ``device``.
+the reference's complex128 path; "fp32" is the fast form), ``device``,
+``grid_budget_bytes`` (device memory for one batch of w-planes).
 ``threads`` and ``verbosity`` are accepted and ignored.
 """
 
@@ -42,6 +43,12 @@ from .base import fused_phase_shift, image_is_canonical
 log = logging.getLogger("rascil-logger")
 
 __all__ = ["predict_ng", "invert_ng", "residual_ng", "predict_gb", "invert_gb", "clear_plan_cache"]
+
+
+def _budget(kwargs):
+    """Device memory for one batch of w-planes (``grid_budget_bytes``, extra
+    keyword; 0 = the library default)."""
+    return int(get_parameter(kwargs, "grid_budget_bytes", 0))
 
 
 def get_parameter(kwargs, key, default=None):
@@ -136,9 +143,10 @@ def _retire(plan, event):
         _spare_ws[:] = keep[-1:]
 
 
-def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, shift):
+def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, shift,
+              budget=0):
     plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=npol,
-                precision=precision, bind=False, phase_shift=shift)
+                precision=precision, bind=False, phase_shift=shift, grid_budget_bytes=budget)
     need = max(plan.workspace_bytes, 256)
     spare = None
     with _plan_lock:
@@ -155,11 +163,12 @@ def _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, s
     return plan
 
 
-def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, shift):
+def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision, shift,
+                   budget=0):
     """(key, (uvw, plan)) for the current stream: the cached plan when it
     fits, else a new one."""
     key = (uvw.device, tuple(uvw.shape), tuple(f.cpu().tolist()), nx, ny, float(pixsize),
-           float(epsilon), bool(do_wstacking), int(npol), precision, tuple(shift))
+           float(epsilon), bool(do_wstacking), int(npol), precision, tuple(shift), int(budget))
     if _cache_on():
         with _plan_lock:
             hit = _plan_cache.pop(key, None)
@@ -171,7 +180,7 @@ def _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precisi
                 return key, (cached_uvw, plan)
             _retire(plan, event)
     return key, (uvw, _new_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol, precision,
-                                shift))
+                                shift, budget))
 
 
 def _checkin_plan(key, entry):
@@ -235,7 +244,7 @@ def predict_ng(bvis, model, **kwargs):
     for ichan, chans in groups:
         f = torch.from_numpy(numpy.ascontiguousarray(freq[chans])).to(device)
         key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, m_npol,
-                                    precision, shift)
+                                    precision, shift, _budget(kwargs))
         try:
             img = _to_device(pixels[ichan], rdt, device)
             vis = entry[1].dirty2ms(img, polmat=pm, npol_vis=vnpol, layout="yx")
@@ -340,7 +349,7 @@ def _invert(bvis, model, dopsf, normalise, residual_of, kwargs):
             return t if (t is None or whole) else t[:, sel, :].contiguous()
 
         key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol,
-                                    precision, shift)
+                                    precision, shift, _budget(kwargs))
         try:
             gvis = pick(vis)
             if residual_of is not None:

@@ -54,7 +54,14 @@ def weight_visibility(vis, model, weighting="uniform", robustness=0.0, **kwargs)
     nchan_img, _, ny, nx = model["pixels"].data.shape
     freq = numpy.asarray(vis.frequency.data, dtype=numpy.float64)
     wcs = model.image_acc.wcs
-    vis_to_im = numpy.round(wcs.sub([4]).wcs_world2pix(freq, 0)[0]).astype(numpy.int32)
+    vis_to_im = numpy.round(wcs.sub([4]).wcs_world2pix(freq, 0)[0]).astype(numpy.int64)
+    # numpy indexing in the reference: negative channels count from the end,
+    # anything else outside the image's channels raises
+    bad = (vis_to_im >= nchan_img) | (vis_to_im < -nchan_img)
+    if bad.any():
+        raise IndexError("visibility channel %d maps to image channel %d of %d"
+                         % (int(numpy.argmax(bad)), int(vis_to_im[bad][0]), nchan_img))
+    vis_to_im = numpy.where(vis_to_im < 0, vis_to_im + nchan_img, vis_to_im).astype(numpy.int32)
     cdelt = wcs.wcs.cdelt
     R = nrows * nbl
     lib = _lib.load()
@@ -70,19 +77,27 @@ def weight_visibility(vis, model, weighting="uniform", robustness=0.0, **kwargs)
         else:
             flags = (flags != 0).to(torch.uint8)
             ftype = _lib.GB_FLAGS_U8
-        grid = torch.empty((nchan_img, npol, ny, nx), dtype=torch.float64, device=device)
+        grid = torch.empty((nchan_img, ny, nx, npol), dtype=torch.float64, device=device)
+        cells = torch.empty((R, nchan), dtype=torch.int32, device=device)
         out = torch.empty((R, nchan, npol), dtype=torch.float64, device=device)
         sums = torch.empty(2, dtype=torch.float64, device=device)
         stream = ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
         _lib.check(lib.gb_weight_visibility(
             _ptr(uvw), _ptr(f), R, nchan, npol, _ptr(v2i), nchan_img, nx, ny,
             float(cdelt[0]), float(cdelt[1]), _ptr(wgt), _ptr(imw), _ptr(flags), ftype,
-            _SCHEMES[weighting], float(robustness), _ptr(grid), _ptr(out), _ptr(sums), stream),
+            _SCHEMES[weighting], float(robustness), _ptr(grid), _ptr(cells), _ptr(out), _ptr(sums),
+            stream),
             "weight_visibility")
-        host = torch.empty(out.shape, dtype=torch.float64, pin_memory=True)
-        host.copy_(out)
-    dst = vis["imaging_weight"].data
-    dst[...] = host.numpy().reshape(dst.shape).astype(dst.dtype, copy=False)
+        dst = vis["imaging_weight"].data
+        res = out.reshape(dst.shape)
+        ddt = torch.from_numpy(numpy.zeros(0, dtype=dst.dtype)).dtype
+        if res.dtype != ddt:
+            res = res.to(ddt)
+        if dst.flags.c_contiguous and dst.flags.writeable:
+            # straight into the caller's array (a DMA when it is page-locked)
+            torch.from_numpy(dst).copy_(res)
+        else:
+            dst[...] = res.cpu().numpy()
     return vis
 
 

@@ -40,6 +40,10 @@ __all__ = ["rsexecute", "invert_list_rsexecute_workflow", "predict_list_rsexecut
            "sum_predict_results_rsexecute", "remove_sumwt"]
 
 DEFAULT_STREAMS = 4
+# Per-block memory for one batch of w-planes when blocks run concurrently
+# (each block's plan holds one batch; the library default of 32 GiB is sized
+# for one large problem on its own).
+CONCURRENT_GRID_BUDGET = 4 << 30
 
 
 class _Rsexecute:
@@ -79,7 +83,10 @@ rsexecute = _Rsexecute()
 
 
 def _streams(kwargs):
-    return int(kwargs.pop("streams", DEFAULT_STREAMS))
+    n = int(kwargs.pop("streams", DEFAULT_STREAMS))
+    if n > 1:
+        kwargs.setdefault("grid_budget_bytes", CONCURRENT_GRID_BUDGET)
+    return n
 
 
 def _map_blocks(func, items, nstreams):

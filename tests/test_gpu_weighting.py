@@ -90,3 +90,28 @@ def test_out_of_grid_raises_like_the_reference_assert():
         weight_visibility(bvis, model, weighting="uniform")
     with pytest.raises(_lib.OutOfGridError):
         weight_visibility(bvis, model, weighting="robust")
+
+
+def test_c_abi_rejects_unmapped_channels():
+    """gb_weight_visibility checks the channel map before any launch."""
+    import ctypes
+    from rascil_gb300 import _lib
+    lib = _lib.load()
+    dev = torch.device("cuda")
+    R, C, P, nci, n = 4, 2, 1, 1, 16
+    uvw = torch.zeros((R, 3), dtype=torch.float64, device=dev)
+    freq = torch.tensor([1e8, 1.1e8], dtype=torch.float64, device=dev)
+    v2i = torch.tensor([0, 1], dtype=torch.int32, device=dev)  # channel 1 -> image channel 1 of 1
+    w = torch.ones((R, C, P), dtype=torch.float64, device=dev)
+    grid = torch.empty((nci, n, n, P), dtype=torch.float64, device=dev)
+    cells = torch.empty((R, C), dtype=torch.int32, device=dev)
+    out = torch.empty_like(w)
+    sums = torch.empty(2, dtype=torch.float64, device=dev)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    rc = lib.gb_weight_visibility(p(uvw), p(freq), R, C, P, p(v2i), nci, n, n, -0.1, 0.1, p(w),
+                                  p(w), None, _lib.GB_FLAGS_NONE, _lib.GB_WEIGHT_UNIFORM, 0.0,
+                                  p(grid), p(cells), p(out), p(sums),
+                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == _lib.GB_ERR_INVALID_ARG
+    assert b"image channel 1" in lib.gb_last_error_string()
+

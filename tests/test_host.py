@@ -216,3 +216,17 @@ def test_es_table_kernel_choice_is_monotone():
         errs = [e for (ss, w, b, e) in rows if ss == s]
         assert len(errs) == 13
         assert errs[-1] < errs[0] * 1e-6
+
+
+def test_weighting_rejects_channels_outside_the_image():
+    """A visibility channel that maps outside the image's channels raises
+    before any device work, as the reference's numpy indexing does."""
+    from rascil_gb300 import data_models as dm
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.imaging import weight_visibility
+    uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
+    f = numpy.array([1.0e8, 1.5e8])
+    b = sim.make_blockvisibility(uvw, f, pc, cfg)
+    model = dm.create_image(64, 1e-3, pc, frequency=[1.0e8], channel_bandwidth=[1e6])
+    with pytest.raises(IndexError):
+        weight_visibility(b, model)
