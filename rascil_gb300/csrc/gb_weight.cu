@@ -8,8 +8,10 @@
 //              are added to the grid with FP64 atomics (gridding.py:260-306);
 //   k_wsums    sum(G) and sum(G^2) over the grid (the robust factor:
 //              sum(G) equals the sum of all flagged imaging weights);
+//   k_wrecip   each cell's divisor inverted once, in place: 1 / G (uniform)
+//              or 1 / (1 + f2 G) (robust), 0 where G <= 0;
 //   k_wapply   the new imaging weight of every sample (gridding.py:332-425)
-//              from its stored cell.
+//              from its stored cell: two products per sample.
 //
 // The grid is [image channel][v][u][pol]: the pols of a cell share one
 // 32-byte sector, so a sample's atomics and its gather touch one sector.
@@ -18,6 +20,7 @@
 // order ((u - 0) / cdelt_u + crpix) - 1 then round-half-to-even, so it is
 // bit-identical to the CPU restatement (and to the reference's linear WCS).
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <vector>
 
@@ -29,15 +32,38 @@ struct WeightGeom {
   int64_t R;
   int C, P, nx, ny, nci;
   double cdu, cdv;      // uv grid cell size (wavelengths; u negative for RA)
+  double rcdu, rcdv;    // their reciprocals
   double crpu, crpv;    // 1-based reference pixel
   const int *vis_to_im;
   int ftype;
 };
 
+// numpy.nan_to_num: NaN -> 0, +-inf -> +-DBL_MAX.  Tested on the exponent
+// bits (integer instructions: every FP64 instruction costs a warp 16 cycles
+// of the SM's FP64 pipe on this part, and these kernels are bound by it).
 __device__ __forceinline__ double nan_to_num(double x) {
-  if (isnan(x)) return 0.0;
-  if (isinf(x)) return x > 0 ? DBL_MAX : -DBL_MAX;
-  return x;
+  const long long b = __double_as_longlong(x);
+  if (((b >> 52) & 0x7ff) != 0x7ff) return x;
+  if (b & 0xfffffffffffffLL) return 0.0;
+  return b < 0 ? -DBL_MAX : DBL_MAX;
+}
+
+// Grid index rint((x / cd + crp) - 1), rounded half to even, equal to what
+// that IEEE sequence gives, or INT_MIN past 2^20 cells (off any grid).  The
+// fast form fma(x, 1 / cd, crp - 1) differs from the IEEE sequence by under
+// 6e-10 for |t| < 2^20 (the reciprocal's rounding, one rounding here, three
+// there), which can change the rounding only that close to a half-integer;
+// within 4e-9 of one the IEEE sequence itself is taken.  Four FP64
+// instructions on the common path instead of a division's dozen.
+__device__ __forceinline__ int grid_index(double x, double cd, double rcd, double crp) {
+  double t = fma(x, rcd, crp - 1.0);
+  double n = rint(t);
+  if (!(fabs(t) < 1048576.0) || fabs(t - n) > 0.5 - 4e-9) {
+    t = gb_sub(gb_add(gb_div(x, cd), crp), 1.0);
+    n = rint(t);
+    if (!(fabs(n) < 1048576.0)) return INT_MIN;
+  }
+  return (int)n;
 }
 
 // Cell (pu, pv) of row r at k = f / c; false if it lies outside the grid.
@@ -45,18 +71,30 @@ __device__ __forceinline__ bool weight_cell(const WeightGeom &w, const double *_
                                             double k, int64_t r, int &pu, int &pv) {
   const double u = nan_to_num(gb_mul(uvw[3 * r], k));
   const double v = nan_to_num(gb_mul(uvw[3 * r + 1], k));
-  const double xu = rint(gb_sub(gb_add(gb_div(u, w.cdu), w.crpu), 1.0));
-  const double xv = rint(gb_sub(gb_add(gb_div(v, w.cdv), w.crpv), 1.0));
-  if (!(xu >= 0.0 && xu < (double)w.nx && xv >= 0.0 && xv < (double)w.ny)) return false;
-  pu = (int)xu;
-  pv = (int)xv;
-  return true;
+  pu = grid_index(u, w.cdu, w.rcdu, w.crpu);
+  pv = grid_index(v, w.cdv, w.rcdv, w.crpv);
+  return pu >= 0 && pu < w.nx && pv >= 0 && pv < w.ny;
 }
 
-__device__ __forceinline__ double flag_factor(const void *flags, int ftype, int64_t i) {
-  if (ftype == GB_FLAGS_I64) return (double)(1 - reinterpret_cast<const long long *>(flags)[i]);
-  if (ftype == GB_FLAGS_U8) return (double)(1 - (int)reinterpret_cast<const uint8_t *>(flags)[i]);
-  return 1.0;
+// Flag values other than 0 and 1, out of line: a predicated inline form
+// would issue its FP64 conversion and product for every sample.
+__device__ __noinline__ double flagged_general(double x, long long f) {
+  return x * (double)(1 - f);
+}
+
+// x * (1 - flag), as the reference forms the flagged imaging weight, in
+// integer instructions for flags 0 and 1: x * 1.0 == x; x * 0.0 is a zero
+// of x's sign, or NaN for x infinite or NaN.
+__device__ __forceinline__ double flagged(double x, const void *flags, int ftype, int64_t i) {
+  long long f = 0;
+  if (ftype == GB_FLAGS_I64) f = reinterpret_cast<const long long *>(flags)[i];
+  else if (ftype == GB_FLAGS_U8) f = reinterpret_cast<const uint8_t *>(flags)[i];
+  if (f == 0) return x;
+  if (f != 1) return flagged_general(x, f);
+  const long long b = __double_as_longlong(x);
+  const bool finite = ((b >> 52) & 0x7ff) != 0x7ff;
+  return __longlong_as_double(finite ? (b & (long long)0x8000000000000000ULL)
+                                     : 0x7ff8000000000000LL);
 }
 
 constexpr uint32_t kNoCell = 0xffffffffu;
@@ -104,7 +142,7 @@ __global__ void k_wgrid(const WeightGeom w, const double *__restrict__ uvw,
     double *g = grid + ((int64_t)w.vis_to_im[c] * w.ny * w.nx + cell) * w.P;
     for (int p = 0; p < w.P; ++p) {
       const int64_t j = i * w.P + p;
-      atomicAdd(&g[p], imw[j] * flag_factor(flags, w.ftype, j));
+      atomicAdd(&g[p], flagged(imw[j], flags, w.ftype, j));
     }
   }
 }
@@ -139,13 +177,24 @@ __global__ void k_wsums(const double *__restrict__ grid, int64_t n, double *__re
   }
 }
 
+__global__ void k_wrecip(double *__restrict__ grid, int64_t n, const double *__restrict__ sums,
+                         int scheme, double a2) {
+  // robust: f2 = (5 10^-R)^2 sum(w) / sum(G^2), with a2 = (5 10^-R)^2 from the host
+  const double f2 = scheme == GB_WEIGHT_ROBUST ? a2 * sums[0] / sums[1] : 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double g = grid[i];
+    if (g > 0.0) grid[i] = recip_pos(scheme == GB_WEIGHT_ROBUST ? 1.0 + f2 * g : g);
+    else if (g != 0.0) grid[i] = 0.0;
+  }
+}
+
 __global__ void k_wapply(const WeightGeom w, const uint32_t *__restrict__ cells,
                          const double *__restrict__ imw, const double *__restrict__ wgt,
                          const void *__restrict__ flags, const double *__restrict__ grid,
                          const double *__restrict__ sums, int scheme, double a2,
                          double *__restrict__ out) {
   const int64_t n = w.R * w.C;
-  // robust: f2 = (5 10^-R)^2 sum(w) / sum(G^2), with a2 = (5 10^-R)^2 from the host
   const double f2 = scheme == GB_WEIGHT_ROBUST ? a2 * sums[0] / sums[1] : 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -159,13 +208,12 @@ __global__ void k_wapply(const WeightGeom w, const uint32_t *__restrict__ cells,
         grid + (cell != kNoCell ? ((int64_t)w.vis_to_im[c] * w.ny * w.nx + cell) * w.P : 0);
     for (int p = 0; p < w.P; ++p) {
       const int64_t j = i * w.P + p;
-      const double x = imw[j] * flag_factor(flags, w.ftype, j);
-      const double g = cell != kNoCell ? gp[p] : 0.0;
+      const double x = flagged(imw[j], flags, w.ftype, j);
+      // the cell's inverted divisor (k_wrecip); positive exactly where G > 0
+      const double rg = cell != kNoCell ? gp[p] : 0.0;
       double y = 0.0;
-      if (g > 0.0) {
-        y = scheme == GB_WEIGHT_UNIFORM ? x * (x * recip_pos(g))
-                                        : x * ((1.0 + f2 * x) * recip_pos(1.0 + f2 * g));
-      }
+      if (__double_as_longlong(rg) > 0)  // rg is a positive double or +0
+        y = scheme == GB_WEIGHT_UNIFORM ? x * (x * rg) : x * ((1.0 + f2 * x) * rg);
       out[j] = y;
     }
   }
@@ -234,6 +282,8 @@ extern "C" int gb_weight_visibility(const double *uvw_dev, const double *freq_de
   w.nci = nchan_img;
   w.cdu = 1.0 / (nx * cdelt_x_deg * d2r);
   w.cdv = 1.0 / (ny * cdelt_y_deg * d2r);
+  w.rcdu = 1.0 / w.cdu;
+  w.rcdv = 1.0 / w.cdv;
   w.crpu = (double)(nx / 2 + 1);
   w.crpv = (double)(ny / 2 + 1);
   w.vis_to_im = vis_to_im_dev;
@@ -269,9 +319,14 @@ extern "C" int gb_weight_visibility(const double *uvw_dev, const double *freq_de
     GB_LAUNCH_CHECK("k_wsums");
   }
   const double a = 5.0 * std::pow(10.0, -robustness);
+  if (weighting != GB_WEIGHT_NATURAL) {
+    ProfScope ps(kProfWeightRecip, s, 16.0 * ngrid);
+    k_wrecip<<<gblocks, kThreads, 0, s>>>(grid_dev, ngrid, sums_dev, weighting, a * a);
+    GB_LAUNCH_CHECK("k_wrecip");
+  }
   {
-    // uniform / robust: imaging weight, flag, grid value in, new weight out;
-    // per (row, channel) its cell
+    // uniform / robust: imaging weight, flag, inverted divisor in, new weight
+    // out; per (row, channel) its cell
     const double per = weighting == GB_WEIGHT_NATURAL ? 16.0 : 24.0 + fb;
     ProfScope ps(kProfWeightApply, s,
                  ns * per + (weighting == GB_WEIGHT_NATURAL ? 0.0 : 4.0 * n));
