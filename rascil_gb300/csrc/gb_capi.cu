@@ -22,6 +22,8 @@ static int make_polmat(const double *host, int nout, int nin, PolMat &pm) {
   for (int i = 0; i < nout * nin; ++i) {
     pm.re[i] = host[2 * i];
     pm.im[i] = host[2 * i + 1];
+    pm.fre[i] = (float)pm.re[i];
+    pm.fim[i] = (float)pm.im[i];
     if (!std::isfinite(pm.re[i]) || !std::isfinite(pm.im[i])) {
       set_error("polarisation matrix holds a non-finite entry");
       return GB_ERR_INVALID_ARG;

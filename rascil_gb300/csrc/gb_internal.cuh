@@ -103,7 +103,26 @@ struct Quad {
 struct PolMat {
   int nout, nin, identity, pad;
   double re[16], im[16];
+  float fre[16], fim[16];  // the same, rounded once on the host for the FP32 kernels
 };
+
+// Element i of the pol matrix in the kernel's real type (the FP32 kernels
+// read the host-rounded copy: a double-to-float conversion is an FP64-pipe
+// instruction, 16 cycles a warp on this part, per item otherwise).
+template <typename R> __device__ __forceinline__ R pm_re(const PolMat &pm, int i);
+template <typename R> __device__ __forceinline__ R pm_im(const PolMat &pm, int i);
+template <> __device__ __forceinline__ float pm_re<float>(const PolMat &pm, int i) {
+  return pm.fre[i];
+}
+template <> __device__ __forceinline__ float pm_im<float>(const PolMat &pm, int i) {
+  return pm.fim[i];
+}
+template <> __device__ __forceinline__ double pm_re<double>(const PolMat &pm, int i) {
+  return pm.re[i];
+}
+template <> __device__ __forceinline__ double pm_im<double>(const PolMat &pm, int i) {
+  return pm.im[i];
+}
 
 // ---------------------------------------------------------------------
 // Per-item coordinates, FP64, with every rounding step explicit so the

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int p = 0; p < NP; ++p) {
           R re = 0, im = 0;
           for (int q = 0; q < npv; ++q) {
-            const R mr = (R)pm.re[p * pm.nin + q], mi = (R)pm.im[p * pm.nin + q];
+            const R mr = pm_re<R>(pm, p * pm.nin + q), mi = pm_im<R>(pm, p * pm.nin + q);
             re += mr * v[q].x - mi * v[q].y;
             im += mr * v[q].y + mi * v[q].x;
           }
@@ -190,6 +190,7 @@ __global__ void __launch_bounds__(kThreads)
   for (int i = threadIdx.x; i < 2 * NP * L.plane; i += kThreads) acc[i] = 0;
   __shared__ uint32_t s_ci;
   __shared__ double s_red[kWarps];
+  __shared__ R s_scale[2];
   for (;;) {
     if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
     __syncthreads();
@@ -220,14 +221,19 @@ __global__ void __launch_bounds__(kThreads)
       for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
       if (lane == 0) s_red[warp] = m;
       __syncthreads();
-      double S = 0.0;
-      for (int w = 0; w < kWarps; ++w) S += s_red[w];
-      if (S > 0.0) {
-        scale = (R)(FixedAcc<R>::kOne / S);
-        inv = (R)(S / FixedAcc<R>::kOne);
+      // one thread forms the scale (FP64 divisions cost 16 cycles a warp
+      // instruction of the FP64 pipe on this part)
+      if (threadIdx.x == 0) {
+        double S = 0.0;
+        for (int w = 0; w < kWarps; ++w) S += s_red[w];
+        s_scale[0] = S > 0.0 ? (R)(FixedAcc<R>::kOne / S) : (R)0;
+        s_scale[1] = S > 0.0 ? (R)(S / FixedAcc<R>::kOne) : (R)0;
       }
+      __syncthreads();
+      scale = s_scale[0];
+      inv = s_scale[1];
     }
-    __syncthreads();  // s_red and s_ci are reused by the next chunk
+    __syncthreads();  // s_red, s_scale and s_ci are reused by the next chunk
     if constexpr (kCache) {
       const R f = direct ? (R)1 : scale;
       for (int jj = threadIdx.x; jj < n; jj += kThreads) {

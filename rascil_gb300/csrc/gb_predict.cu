@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(kThreads)
             R re = 0, im = 0;
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-              const R mr = (R)pm.re[q * pm.nin + p], mi = (R)pm.im[q * pm.nin + p];
+              const R mr = pm_re<R>(pm, q * pm.nin + p), mi = pm_im<R>(pm, q * pm.nin + p);
               re += mr * v[p].x - mi * v[p].y;
               im += mr * v[p].y + mi * v[p].x;
             }
@@ -312,13 +312,22 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// float2 elements from one staged row to the next in k_degrid_lane: SW
+// cells padded to an odd count, plus one 16-byte unit for NP = 4.
+__host__ __device__ constexpr int lane_row(int NP, int SW) {
+  return (SW | 1) * NP + (NP == 4 ? 2 : 0);
+}
+
 // FP32 degridder, one item per thread.  A CTA takes a chunk (up to 256
 // items of one bucket); thread i owns item i: its u and v kernel values
 // (with the checkerboard sign (-1)^(p+q) folded in) stay in registers for
 // all planes, and for every plane the thread sums its whole W x W footprint
 // from the plane's staged sub-grid ([SW][pitch][NP] complex, a cell's pols
 // contiguous), double-buffered with cp.async so plane k + 1 streams in
-// while plane k is summed.
+// while plane k is summed.  Staged rows are lane_row(NP, SW) float2 apart:
+// an odd number of 16-byte units for NP = 4 (whose cells are two 16-byte
+// units), so one load instruction's 32 cells spread over all eight 16-byte
+// bank groups instead of the four of one parity.
 // Per item-plane that is W^2 NP shared loads and 2 W^2 NP FMAs with no
 // cross-lane reduction, against the warp-per-item map of k_degrid.
 template <int NP, int WT>
@@ -330,9 +339,9 @@ __global__ void __launch_bounds__(kThreads, 2)
                   uint32_t *__restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int T = g.T;
-  const int SW = T + WT - 1, pitch = SW | 1, pstride = SW * pitch;
-  float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][pitch][NP]
-  float *skv = reinterpret_cast<float *>(stage + 2 * NP * pstride);  // [WT][kThreads]: own kv
+  const int SW = T + WT - 1, rowf2 = lane_row(NP, SW), pstride = SW * rowf2;
+  float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][rowf2]
+  float *skv = reinterpret_cast<float *>(stage + 2 * pstride);   // [WT][kThreads]: own kv
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float scale_u = 2.f / (float)WT;
   const float beta = (float)g.beta;
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         int q = tv * T + y;
         while (q >= g.ngy) q -= g.ngy;
         const float2 *src = gp + pol * plane + (int64_t)rp.row(q) * g.ngx;
-        float2 *d = dst + y * pitch * NP + pol;
+        float2 *d = dst + y * rowf2 + pol;
         for (int x = lane; x < SW; x += 32) {
           int pc = tu * T + x;
           while (pc >= g.ngx) pc -= g.ngx;
@@ -396,12 +405,12 @@ __global__ void __launch_bounds__(kThreads, 2)
     for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
     for (int k = k_lo; k < k_hi; ++k) {
       const float2 *gp = grid + (int64_t)(k - b0) * NP * plane;
-      const float2 *sg = stage + ((k - k_lo) & 1) * NP * pstride;
+      const float2 *sg = stage + ((k - k_lo) & 1) * pstride;
       if (!direct) {
         // plane k + 1 goes to the other buffer (consumed in iteration k - 1,
         // released by that iteration's closing barrier)
         if (k + 1 < k_hi) {
-          stage_plane(k + 1, stage + ((k + 1 - k_lo) & 1) * NP * pstride);
+          stage_plane(k + 1, stage + ((k + 1 - k_lo) & 1) * pstride);
           cp_async_wait1();
         } else {
           cp_async_wait0();
@@ -436,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             }
           } else {
             // a cell's NP values are contiguous: 16-byte loads of two pols
-            const float2 *row = sg + ((lv + b) * pitch + lu) * NP;
+            const float2 *row = sg + (lv + b) * rowf2 + lu * NP;
 #pragma unroll
             for (int a = 0; a < WT; ++a) {
               if constexpr (NP == 1) {
@@ -489,7 +498,7 @@ __global__ void __launch_bounds__(kThreads, 2)
           float re = 0.f, im = 0.f;
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
-            const float mr = (float)pm.re[q * pm.nin + p], mi = (float)pm.im[q * pm.nin + p];
+            const float mr = pm.fre[q * pm.nin + p], mi = pm.fim[q * pm.nin + p];
             re += mr * v[p].x - mi * v[p].y;
             im += mr * v[p].y + mi * v[p].x;
           }
@@ -515,7 +524,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 
 size_t degrid_lane_smem_bytes(const gb_plan *p) {
   const int SW = p->g.T + p->g.W - 1;
-  return (size_t)2 * p->g.NP * SW * (SW | 1) * sizeof(float2) +
+  return (size_t)2 * SW * lane_row(p->g.NP, SW) * sizeof(float2) +
          (size_t)p->g.W * kThreads * sizeof(float);
 }
 
