@@ -289,7 +289,9 @@ int gb_wrange_noalloc(const double *uvw_dev, const double *freq_dev, int64_t nro
  *   weight_dev, imaging_weight_dev  [nrows][nchan][npol] f64
  *   flags_dev     [nrows][nchan][npol] of flags_type, or NULL (GB_FLAGS_NONE)
  *   cdelt_x_deg, cdelt_y_deg  the image WCS's cdelt[0], cdelt[1] (degrees)
- *   grid_dev      [nchan_img][ny][nx][npol] f64 scratch: the gridded weights on return
+ *   grid_dev      [nchan_img][ny][nx][npol] f64 scratch: on return the gridded weights G
+ *                 (natural), else per cell 1 / G (uniform) or 1 / (1 + f2 G) (robust), 0
+ *                 where G <= 0
  *   cells_dev     [nrows][nchan] u32 scratch: each sample's cell v * nx + u
  *   imaging_weight_out_dev  [nrows][nchan][npol] f64 (may alias neither input)
  *   sums_dev      [2] f64: sum(G), sum(G^2) on return

@@ -61,7 +61,7 @@ const char *kProfNames[kProfCount] = {
     "k_prep_image", "k_screen_pad", "cufft_forward", "k_degrid", "k_dft_components",
     "k_dft_pixels", "k_col_a_inv", "k_col_b_inv", "k_col_a_pred", "k_col_b_pred",
     "zero_margins", "k_rows_inverse", "k_rows_forward", "grid_zero",
-    "k_wgrid", "k_wsums", "k_wapply", "k_rotate"};
+    "k_wgrid", "k_wsums", "k_wapply", "k_wrecip", "k_rotate"};
 
 bool prof_on() {
   std::lock_guard<std::mutex> lk(g_mu);

@@ -34,6 +34,7 @@ enum ProfId {
   kProfWeightGrid,
   kProfWeightSums,
   kProfWeightApply,
+  kProfWeightRecip,
   kProfRotate,
   kProfCount
 };
