@@ -798,9 +798,23 @@ def dist_setup(args):
     import torch.distributed as dist
     rank = int(os.environ["RANK"])
     world = int(os.environ["WORLD_SIZE"])
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
     dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world
+
+
+def max_over_ranks(x, world):
+    """The slowest rank's value (every rank gets it): the job's step time is
+    the max over ranks.  NCCL reduces a CUDA tensor, gloo a CPU one."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def run_reference(args):
@@ -882,10 +896,7 @@ def main():
         torch.distributed.barrier()
     ms, out, clocks, stats = time_steps(wl, "fp32", wl.vis32, wl.wgt32, wl.model32, args.steps,
                                         args.warmup, sampler=sampler, profile=True)
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world)
     dirty, pred, info = out
     value = world * 2 * wl.nvis / (ms * 1e-3) / 1e6
     acc32 = accuracy(wl, dirty, pred, "fp32")
