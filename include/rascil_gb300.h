@@ -307,6 +307,22 @@ int gb_weight_visibility(const double *uvw_dev, const double *freq_dev, int64_t 
                          double *grid_dev, uint32_t *cells_dev,
                          double *imaging_weight_out_dev, double *sums_dev, void *stream);
 
+/* A list of independent solves (many snapshots of uneven size) issued in
+ * one call: plan i is bound to workspace i % nslots and runs on stream
+ * i % nslots -- its bucket sort, then ms2dirty of vis[i] into dirty[i] and
+ * dirty2ms of model[i] into pred[i] (either may be NULL, arrays included),
+ * with unit weights, no flags and the identity pol matrix -- so the slots'
+ * work overlaps while each slot's plans run in order on their shared
+ * workspace.  Each workspace holds at least the largest workspace_size of
+ * its plans.  Asynchronous; capturable in a CUDA graph.  Replaces the
+ * reference's per-snapshot Dask tasks over invert/predict
+ * (workflows/rsexecute/imaging/imaging_rsexecute.py:72-157) for a list of
+ * blocks already on the device. */
+int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
+                 const size_t *workspace_bytes, void *const *streams, int32_t nslots,
+                 const void *const *vis, void *const *dirty, const void *const *model,
+                 void *const *pred, int32_t layout);
+
 /* Tangent-plane phase rotation of visibilities in place, RASCIL's
  * phaserotate_visibility(tangent=True) (visibility/base.py:296-357) with
  * the phasor of calculate_blockvisibility_phasor (:1248-1264):

@@ -100,6 +100,8 @@ SIGNATURES = {
                                         _c.c_double, _vp, _vp, _vp, _c.c_int32, _c.c_int32,
                                         _c.c_double, _vp, _vp, _vp, _vp, _vp]),
     "gb_plan_device_status": (_c.c_int, [_vp, _vp, _c.POINTER(_c.c_int32)]),
+    "gb_batch_run": (_c.c_int, [_vp, _c.c_int32, _vp, _vp, _vp, _c.c_int32, _vp, _vp, _vp,
+                                _vp, _c.c_int32]),
     "gb_phase_rotate": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32, _vp,
                                    _c.c_int32, _c.c_double, _c.c_double, _c.c_double,
                                    _c.c_int32, _vp]),

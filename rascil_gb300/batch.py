@@ -72,6 +72,45 @@ class SnapshotBatch:
             for s in streams:
                 main.wait_stream(s)
 
+    def run_native(self, vis, models):
+        """run(vis, models) issued by the library in one call
+        (``gb_batch_run``): the same plans, slots and streams, without a
+        Python round trip per snapshot."""
+        import ctypes
+
+        from . import _lib
+        n = len(self.plans)
+        if len(vis) != n or len(models) != n:
+            raise ValueError("one vis and one model per snapshot")
+        for i, p in enumerate(self.plans):
+            v, m = vis[i], models[i]
+            if (not v.is_cuda or v.dtype != p.complex_dtype or not v.is_contiguous()
+                    or v.numel() != p.nrows * p.nchan * p.npol):
+                raise ValueError("vis[%d] must be a contiguous %s CUDA tensor of %d values"
+                                 % (i, p.complex_dtype, p.nrows * p.nchan * p.npol))
+            if (not m.is_cuda or m.dtype != p.real_dtype or not m.is_contiguous()
+                    or m.numel() != p.npol * p.npix_x * p.npix_y):
+                raise ValueError("models[%d] must be a contiguous %s CUDA tensor of %d values"
+                                 % (i, p.real_dtype, p.npol * p.npix_x * p.npix_y))
+        main = torch.cuda.current_stream(self.device)
+        for s in self.streams:
+            s.wait_stream(main)
+        ptrs = ctypes.c_void_p * n
+        slots = ctypes.c_void_p * self.nslots
+        args = (ptrs(*[p._handle.value for p in self.plans]), n,
+                slots(*[w.data_ptr() for w in self.workspaces]),
+                (ctypes.c_size_t * self.nslots)(*[w.numel() for w in self.workspaces]),
+                slots(*[s.cuda_stream for s in self.streams]), self.nslots,
+                ptrs(*[t.data_ptr() for t in vis]), ptrs(*[t.data_ptr() for t in self.dirty]),
+                ptrs(*[t.data_ptr() for t in models]), ptrs(*[t.data_ptr() for t in self.pred]),
+                _lib.GB_LAYOUT_YX)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().gb_batch_run(*args), "gb_batch_run")
+        for i, p in enumerate(self.plans):
+            p.workspace = self.workspaces[i % self.nslots]
+        for s in self.streams:
+            main.wait_stream(s)
+
     def capture(self, vis, models):
         """Record run(vis, models) as a CUDA graph; replay() re-runs it."""
         self.run(vis, models)  # warm-up outside capture (cuFFT, caches)

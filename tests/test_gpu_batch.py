@@ -76,3 +76,29 @@ def test_graph_capture_and_replay_on_new_data():
     for a, d in zip(first, b.dirty):
         assert rel_rms(d.cpu().numpy(), 2.0 * a.cpu().numpy()) < 1e-5
     b.close()
+
+
+def test_native_batch_call_matches_python_loop():
+    """gb_batch_run (one library call for the whole list) gives run()'s
+    images and visibilities; malformed inputs are refused before any launch."""
+    from rascil_gb300.batch import SnapshotBatch
+    snaps, vis, models = _snapshots(9, precision="fp32")
+    b = SnapshotBatch(snaps, 1e-5, precision="fp32", nslots=4)
+    b.run(vis, models)
+    torch.cuda.synchronize()
+    dirty = [d.clone() for d in b.dirty]
+    pred = [v.clone() for v in b.pred]
+    for d in b.dirty:
+        d.zero_()
+    for v in b.pred:
+        v.zero_()
+    b.run_native(vis, models)
+    torch.cuda.synchronize()
+    for a, d in zip(dirty, b.dirty):
+        assert rel_rms(d.cpu().numpy(), a.cpu().numpy()) < 1e-5
+    for a, v in zip(pred, b.pred):
+        assert rel_rms(v.cpu().numpy(), a.cpu().numpy()) < 1e-5
+    with pytest.raises(ValueError):
+        b.run_native(vis[:-1] + [vis[-1][:-1]], models)
+    b.close()
+
