@@ -22,6 +22,15 @@ kernel, the GPU clocks seen during the timed region and the CPU baseline
 (the oracle's multithreaded C gridder on a bounded sample).
 
 ``--impl reference`` times the reference path's CPU stand-in alone.
+
+``--path`` selects a path either side of the imaging step instead, each
+with its own JSON line (device-timed rate, per-kernel GB/s, an end-to-end
+rate through the public API with page-locked host arrays, and a timed CPU
+oracle sample): ``weights`` (weight_visibility, uniform, over every sample
+of the workload), ``rotation`` (gb_phase_rotate over the workload's
+visibilities, and the imaging step with the rotation fused in against the
+centred step), ``lists`` (invert_list / residual_list over 256 uneven
+snapshots, at 1, 4 and 8 streams, with the device-busy time of one pass).
 """
 import argparse
 import json
