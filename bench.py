@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
-    ap.add_argument("--config", default="c2")
+    ap.add_argument("--config", default="low-like")
     ap.add_argument("--scale", default="full", choices=list(SCALES))
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=1)
@@ -670,7 +670,7 @@ def bench_rotation(args):
 
 
 def bench_lists(args):
-    """invert_list / residual_list over 256 uneven snapshots (config 3:
+    """invert_list / residual_list over 256 uneven snapshots (the batched configuration:
     32-512 antennas, 1-8 channels, 1-16 times, 256-2048 pixel images),
     page-locked host BlockVisibility per snapshot, FP32 form at eps 1e-5.
     Timed with the host clock: every call ends with its results on the host."""

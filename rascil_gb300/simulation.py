@@ -75,29 +75,29 @@ def pixel_sources(rng, nsrc, npixel, cellsize, max_offset):
 
 CONFIGS = {
     # Plain FP64 invert + predict round trip (CPU-runnable size)
-    "c1": dict(nants=64, layout=(("disk", 64, 1000.0),), lat=-26.7, dec=-45.0,
+    "small-array": dict(nants=64, layout=(("disk", 64, 1000.0),), lat=-26.7, dec=-45.0,
                freq=(100e6, 100e6, 1), ntimes=64, ha=(-2.0, 2.0), pol="stokesI",
                image_pol="stokesI", nsrc=20, flux=("uniform", 0.1, 1.0), offset=4.0,
                noise=0.0, npixel=512, cellsize=5e-4, epsilon=1e-12, dtype="c16"),
     # LOW-like: FP32 form vs plain FP64 form
-    "c2": dict(layout=(("disk", 224, 2000.0), ("lograd", 288, 2000.0, 35000.0)), lat=-26.7,
+    "low-like": dict(layout=(("disk", 224, 2000.0), ("lograd", 288, 2000.0, 35000.0)), lat=-26.7,
                dec=-30.0, freq=(100e6, 200e6, 16), ntimes=128, ha=(-3.0, 3.0), pol="linear",
                image_pol="stokesIQUV", nsrc=1000, flux=("powerlaw", 0.01, 1.0, 1.7),
                offset=2.0, noise=0.01, npixel=8192, cellsize=1e-5, epsilon=1e-5, dtype="c8"),
-    # Differentiable predict geometry: 128-antenna subset of c1's law
-    "c4": dict(layout=(("disk", 128, 1000.0),), lat=-26.7, dec=-45.0,
+    # Differentiable predict geometry: 128 antennas drawn by the small array's law
+    "gain-solve": dict(layout=(("disk", 128, 1000.0),), lat=-26.7, dec=-45.0,
                freq=(150e6, 158e6, 8), ntimes=64, ha=(-2.0, 2.0), pol="stokesI",
                image_pol="stokesI", nsrc=200, flux=("uniform", 0.01, 1.0), offset=4.0,
                noise=0.0, npixel=2048, cellsize=5e-4 / 4, epsilon=1e-5, dtype="c8"),
     # MID-like wide-field stress test
-    "c5": dict(layout=(("disk", 64, 1000.0), ("lograd", 133, 1000.0, 80000.0)), lat=-30.7,
+    "mid-like": dict(layout=(("disk", 64, 1000.0), ("lograd", 133, 1000.0, 80000.0)), lat=-30.7,
                dec=-60.0, freq=(0.95e9, 1.67e9, 64), ntimes=512, ha=(-4.0, 4.0), pol="linear",
                image_pol="stokesIQUV", nsrc=5000, flux=("uniform", 0.01, 1.0), offset=0.2,
                noise=0.0, npixel=16384, cellsize=5e-7, epsilon=1e-5, dtype="c8"),
 }
 
 
-def observation(name="c1", seed=0, ntimes=None, nchan=None, npixel=None, nants=None):
+def observation(name="small-array", seed=0, ntimes=None, nchan=None, npixel=None, nants=None):
     """Geometry of a named configuration: (uvw [ntimes, nbl, 3], freq,
     phasecentre, config dict).  Optional overrides shrink the case."""
     cfg = dict(CONFIGS[name])

@@ -20,7 +20,7 @@ def main(ntimes=2):
     from oracle import ref_dft
     from rascil_gb300 import simulation as sim
     from rascil_gb300.dft import dft_components
-    uvw, freq, pc, cfg = sim.observation("c2", ntimes=ntimes)
+    uvw, freq, pc, cfg = sim.observation("low-like", ntimes=ntimes)
     src = sim.sources(cfg)
     lmn = sim.lmn_rows(src)
     flux = sim.component_fluxes(cfg, src, len(freq))
@@ -53,7 +53,7 @@ def main(ntimes=2):
     c = fast.reshape(ref.shape).cpu().numpy().astype(numpy.complex128)
     nvis = b.size
     print(json.dumps({
-        "workload": "c2 geometry, %d times x %d baselines x %d chan x %d pol, %d components"
+        "workload": "LOW-like geometry, %d times x %d baselines x %d chan x %d pol, %d components"
                     % (ntimes, uvw.shape[1], len(freq), flux.shape[-1], len(lmn)),
         "reference_dft_kernel_ms": round(t_ref, 3),
         "gb_dft_exact_fp64_ms": round(t_ours, 3),

@@ -45,7 +45,7 @@ def _reference_worker(rank, world, port, q):
     import torch.distributed as dist
 
     import bench
-    args = argparse.Namespace(gpus=world, config="c1", scale="tiny", warmup=3, steps=1,
+    args = argparse.Namespace(gpus=world, config="small-array", scale="tiny", warmup=3, steps=1,
                               cpu_planes=1)
     out = io.StringIO()
     with contextlib.redirect_stdout(out):

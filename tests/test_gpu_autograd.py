@@ -16,7 +16,7 @@ def _case(precision="fp64", nants=24, ntimes=6, nchan=3, npix=96, seed=0):
     from rascil_gb300 import simulation as sim
     from rascil_gb300.wgridder import Plan
     from rascil_gb300.autograd import baseline_antennas
-    uvw, freq, pc, cfg = sim.observation("c4", seed=seed, ntimes=ntimes, nchan=nchan,
+    uvw, freq, pc, cfg = sim.observation("gain-solve", seed=seed, ntimes=ntimes, nchan=nchan,
                                          nants=nants)
     cell = 2.0e-4
     u = torch.from_numpy(uvw.reshape(-1, 3).copy()).cuda()

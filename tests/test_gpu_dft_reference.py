@@ -14,7 +14,7 @@ def test_component_dft_matches_reference_cuda_kernel():
         pytest.skip("reference kernel source not extracted (no reference tree at build time)")
     from rascil_gb300 import simulation as sim
     from rascil_gb300.dft import dft_components
-    uvw, freq, pc, cfg = sim.observation("c2", ntimes=2, nchan=5, nants=64)
+    uvw, freq, pc, cfg = sim.observation("low-like", ntimes=2, nchan=5, nants=64)
     cfg["nsrc"] = 37
     src = sim.sources(cfg)
     lmn = sim.lmn_rows(src)

@@ -19,7 +19,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def _obs(name="c1", ntimes=8, nchan=None, zerow=False, npixel=None, pol=None, image_pol=None,
+def _obs(name="small-array", ntimes=8, nchan=None, zerow=False, npixel=None, pol=None, image_pol=None,
          nants=None):
     from rascil_gb300 import simulation as sim
     uvw, freq, pc, cfg = sim.observation(name, seed=0, ntimes=ntimes, nchan=nchan,
@@ -73,8 +73,9 @@ def test_psf_peak_is_one():
     assert sumwt[0, 0] == uvw.shape[0] * uvw.shape[1] * len(freq)
 
 
-def _c1_data(precision, ntimes=64):
-    """Config-1 geometry with visibilities of its 20 sources (exact FP64 DFT)."""
+def _small_array_data(precision, ntimes=64):
+    """The small array (64 antennas in a 1 km disk) with visibilities of its 20 sources
+    (exact FP64 DFT)."""
     from rascil_gb300 import simulation as sim
     from rascil_gb300.dft import dft_components
     uvw, freq, pc, cfg = _obs(ntimes=ntimes)
@@ -92,11 +93,11 @@ def _c1_data(precision, ntimes=64):
 
 
 @pytest.mark.parametrize("precision,eps,tol", [("fp64", 1e-12, 1e-10), ("fp32", 1e-5, 1e-5)])
-def test_config1_invert_matches_exact_dft(precision, eps, tol):
-    """Config 1 at full size: 64 ants, 64 times, 512^2, w-stacking."""
+def test_small_array_invert_matches_exact_dft(precision, eps, tol):
+    """The small array at full size: 64 ants, 64 times, 512^2, w-stacking."""
     from rascil_gb300.dft import dft_pixels
     from rascil_gb300.imaging import invert_ng
-    uvw, freq, pc, cfg, src, bvis, model, u, f = _c1_data(precision)
+    uvw, freq, pc, cfg, src, bvis, model, u, f = _small_array_data(precision)
     im, sumwt = invert_ng(bvis, model, epsilon=eps, precision=precision)
     got = im["pixels"].data[0, 0] * sumwt[0, 0]
     npix, cell = cfg["npixel"], cfg["cellsize"]
@@ -116,9 +117,9 @@ def test_config1_invert_matches_exact_dft(precision, eps, tol):
 
 
 @pytest.mark.parametrize("precision,eps,tol", [("fp64", 1e-12, 1e-10), ("fp32", 1e-5, 1e-5)])
-def test_config1_predict_matches_exact_dft(precision, eps, tol):
+def test_small_array_predict_matches_exact_dft(precision, eps, tol):
     from rascil_gb300.imaging import predict_ng
-    uvw, freq, pc, cfg, src, bvis, model, u, f = _c1_data(precision)
+    uvw, freq, pc, cfg, src, bvis, model, u, f = _small_array_data(precision)
     got = predict_ng(bvis, model, epsilon=eps, precision=precision)["vis"].data
     truth = bvis["vis"].data.astype(numpy.complex128)  # exact DFT of the same sources
     assert rel_rms(got, truth) < tol
@@ -131,7 +132,7 @@ def test_per_channel_path_and_flags():
     from rascil_gb300.data_models import create_image
     from rascil_gb300.imaging import invert_ng
     from rascil_gb300.polarisation import PolarisationFrame
-    uvw, freq, pc, cfg = _obs("c4", ntimes=4, nchan=3, npixel=64, nants=32)
+    uvw, freq, pc, cfg = _obs("gain-solve", ntimes=4, nchan=3, npixel=64, nants=32)
     cfg["cellsize"] = 2e-3
     rng = numpy.random.default_rng(5)
     shape = uvw.shape[:2] + (3, 1)
@@ -177,7 +178,7 @@ def test_plan_cache_reuse_and_invalidation(monkeypatch):
     the calls are noticed (the cached plan is rebuilt, not reused)."""
     from rascil_gb300.imaging import invert_ng, predict_ng
     from rascil_gb300.imaging import ng
-    uvw, freq, pc, cfg, src, bvis, model, u, f = _c1_data("fp32", ntimes=16)
+    uvw, freq, pc, cfg, src, bvis, model, u, f = _small_array_data("fp32", ntimes=16)
     kw = dict(epsilon=1e-5, precision="fp32")
     ng.clear_plan_cache()
     monkeypatch.setenv("RASCIL_GB300_PLAN_CACHE", "1")

@@ -100,7 +100,7 @@ def test_shift_vis_to_image_to_offset_image_centre():
     from rascil_gb300 import simulation as sim
     from rascil_gb300.data_models import SkyDirection
     from rascil_gb300.imaging.base import lmn_of, shift_vis_to_image
-    uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=1)
     b = sim.make_blockvisibility(uvw, f, pc, cfg)
     b["vis"].data[...] = 1.0
     off = SkyDirection(pc.ra.rad + 0.01, pc.dec.rad - 0.005)
@@ -119,7 +119,7 @@ def test_shift_vis_to_image_to_offset_image_centre():
 def _offset_case(precision, ntimes=16, nchan=3):
     from rascil_gb300 import data_models as dm
     from rascil_gb300 import simulation as sim
-    uvw, freq, pc, cfg = sim.observation("c1", seed=0, ntimes=ntimes, nchan=nchan, npixel=256)
+    uvw, freq, pc, cfg = sim.observation("small-array", seed=0, ntimes=ntimes, nchan=nchan, npixel=256)
     if len(freq) > 1 and freq[0] == freq[-1]:
         freq = numpy.linspace(1.0e8, 1.2e8, nchan)
     rng = numpy.random.default_rng(7)

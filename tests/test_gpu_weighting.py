@@ -61,11 +61,11 @@ def test_weights_match_reference_golden(scheme, rob):
 
 @pytest.mark.parametrize("scheme,rob", CASES)
 def test_weights_larger_case_vs_oracle(scheme, rob):
-    """The small (c1) array, 32 times, 4 channels onto 2 image channels,
+    """The small array, 32 times, 4 channels onto 2 image channels,
     4 pols, 10 % flags, many samples per uv cell."""
     from rascil_gb300 import simulation as sim
     from rascil_gb300.imaging import weight_visibility
-    uvw, _, pc, cfg = sim.observation("c1", seed=3, ntimes=32)
+    uvw, _, pc, cfg = sim.observation("small-array", seed=3, ntimes=32)
     freq = numpy.linspace(1.0e8, 1.2e8, 4)
     rng = numpy.random.default_rng(11)
     shape = uvw.shape[:2] + (len(freq), 4)

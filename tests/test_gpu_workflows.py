@@ -25,10 +25,10 @@ pytestmark = pytest.mark.gpu
 
 
 def _time_blocks(precision, splits=(3, 5, 8), npixel=256, seed=1):
-    """One c1 observation cut into uneven time blocks, random vis and
+    """One small-array observation cut into uneven time blocks, random vis and
     weights, flags on 5 %."""
     from rascil_gb300 import simulation as sim
-    uvw, freq, pc, cfg = sim.observation("c1", seed=0, ntimes=sum(splits), npixel=npixel)
+    uvw, freq, pc, cfg = sim.observation("small-array", seed=0, ntimes=sum(splits), npixel=npixel)
     rng = numpy.random.default_rng(seed)
     dtype = numpy.complex128 if precision == "fp64" else numpy.complex64
     shape = uvw.shape[:2] + (len(freq), 1)

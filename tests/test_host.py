@@ -46,7 +46,7 @@ def test_geometry_matches_reference_golden():
 
 def test_baseline_counts_of_named_configurations():
     from rascil_gb300 import simulation as sim
-    for name, nbl in (("c1", 2016), ("c2", 130816), ("c4", 8128), ("c5", 19306)):
+    for name, nbl in (("small-array", 2016), ("low-like", 130816), ("gain-solve", 8128), ("mid-like", 19306)):
         uvw, f, pc, cfg = sim.observation(name, ntimes=1)
         assert uvw.shape == (1, nbl, 3)
 
@@ -66,7 +66,7 @@ def test_normalise_sumwt_matches_reference_golden():
 def test_blockvisibility_shim_accessors():
     from rascil_gb300 import simulation as sim
     from rascil_gb300.data_models import copy_visibility
-    uvw, f, pc, cfg = sim.observation("c1", ntimes=2)
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=2)
     b = sim.make_blockvisibility(uvw, f, pc, cfg)
     b["vis"].data[...] = 1 + 2j
     b["flags"].data[0, 0, 0, 0] = 1
@@ -82,7 +82,7 @@ def test_blockvisibility_shim_accessors():
 def test_image_wcs_and_phase_centre():
     from rascil_gb300 import simulation as sim
     from rascil_gb300.imaging.base import image_is_canonical, image_phasecentre, separation
-    uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=1)
     im = sim.model_image(cfg, sim.sources(cfg), pc, f)
     assert image_is_canonical(im)
     assert separation(image_phasecentre(im), pc) < 1e-15
@@ -151,7 +151,7 @@ def test_fused_phase_shift_is_the_plan_frame_direction():
     from rascil_gb300 import simulation as sim
     from rascil_gb300.data_models import SkyDirection
     from rascil_gb300.imaging.base import fused_phase_shift, lmn_of
-    uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=1)
     b = sim.make_blockvisibility(uvw, f, pc, cfg)
     im = sim.model_image(cfg, ([], [], [], [], []), pc, f)
     assert fused_phase_shift(b, im) == (False, (0.0, 0.0, 0.0))
@@ -224,7 +224,7 @@ def test_weighting_rejects_channels_outside_the_image():
     from rascil_gb300 import data_models as dm
     from rascil_gb300 import simulation as sim
     from rascil_gb300.imaging import weight_visibility
-    uvw, f, pc, cfg = sim.observation("c1", ntimes=1)
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=1)
     f = numpy.array([1.0e8, 1.5e8])
     b = sim.make_blockvisibility(uvw, f, pc, cfg)
     model = dm.create_image(64, 1e-3, pc, frequency=[1.0e8], channel_bandwidth=[1e6])

@@ -9,7 +9,7 @@ import pytest
 
 def _blocks(n=3):
     from rascil_gb300 import simulation as sim
-    uvw, f, pc, cfg = sim.observation("c1", ntimes=2)
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=2)
     out = []
     for i in range(n):
         b = sim.make_blockvisibility(uvw, f, pc, cfg)
