@@ -230,3 +230,28 @@ def test_weighting_rejects_channels_outside_the_image():
     model = dm.create_image(64, 1e-3, pc, frequency=[1.0e8], channel_bandwidth=[1e6])
     with pytest.raises(IndexError):
         weight_visibility(b, model)
+
+
+def test_copy_visibility_keeps_aliases_and_takes_given_vis():
+    """copy_visibility deep-copies every array once: arrays the input shares
+    (weight and imaging_weight as one array, as natural weighting leaves
+    them) stay shared in the copy and independent of the input; a given vis
+    array becomes the copy's visibilities without a copy."""
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.data_models import BlockVisibility, copy_visibility
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=2)
+    shape = uvw.shape[:2] + (len(f), 1)
+    w = numpy.full(shape, 2.0)
+    b = BlockVisibility(numpy.ones(shape, numpy.complex128), uvw, f, pc,
+                        sim.PolarisationFrame("stokesI"), weight=w, imaging_weight=w)
+    c = copy_visibility(b)
+    assert c["weight"].data is c["imaging_weight"].data
+    assert c["weight"].data is not w
+    c["imaging_weight"].data[...] = 5.0
+    assert numpy.all(w == 2.0) and numpy.all(c["weight"].data == 5.0)
+    given = numpy.zeros(shape, numpy.complex128)
+    d = copy_visibility(b, vis=given)
+    assert d["vis"].data is given and d.uvw.data is not b.uvw.data
+    z = copy_visibility(b, zero=True)
+    assert numpy.all(z["vis"].data == 0) and numpy.all(b["vis"].data == 1)
+    assert c.phasecentre is not None and c.attrs is not b.attrs
