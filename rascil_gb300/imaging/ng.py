@@ -234,6 +234,12 @@ def predict_ng(bvis, model, **kwargs):
     polmat = conversion_matrix(model.image_acc.polarisation_frame,
                                bvis.blockvisibility_acc.polarisation_frame)
     pm = None if numpy.array_equal(polmat, numpy.eye(vnpol)) else polmat
+    if nrows * nbaselines == 0 or vnchan == 0:
+        # no samples to predict: the zeroed copy ng.py:56 starts from
+        newbvis = copy_visibility(bvis, zero=True)
+        if rotates:
+            newbvis.attrs["phasecentre"] = model.image_acc.phasecentre
+        return newbvis
     uvw = _device_uvw(bvis.uvw.data, device, nan_to_num=True)
     pixels = model["pixels"].data
     out = torch.empty((nrows * nbaselines, vnchan, vnpol), dtype=cdt, device=device)
@@ -323,6 +329,11 @@ def _invert(bvis, model, dopsf, normalise, residual_of, kwargs):
         pred_pm = None if numpy.array_equal(pmat, numpy.eye(vnpol)) else pmat
     vis_to_im = _vis_to_im(model, freq)
     R = nrows * nbaselines
+    if R == 0 or vnchan == 0:
+        # no samples: ms2dirty grids nothing, the weight sums stay 0 and
+        # normalise_sumwt leaves a zero image (ng.py:206-208, base.py:109-162)
+        zeros = numpy.zeros(model["pixels"].data.shape, dtype=model["pixels"].data.dtype)
+        return model.copy(deep=True, pixels=zeros), numpy.zeros([nchan, npol])
     uvw = _device_uvw(bvis.uvw.data, device)
     vis = None
     if not dopsf:

@@ -64,6 +64,8 @@ def weight_visibility(vis, model, weighting="uniform", robustness=0.0, **kwargs)
     vis_to_im = numpy.where(vis_to_im < 0, vis_to_im + nchan_img, vis_to_im).astype(numpy.int32)
     cdelt = wcs.wcs.cdelt
     R = nrows * nbl
+    if R == 0 or nchan == 0 or npol == 0:
+        return vis  # no samples: nothing gridded, nothing reweighted
     lib = _lib.load()
     with torch.cuda.device(device):
         uvw = _dev(vis.uvw.data.reshape(R, 3), torch.float64, device)

@@ -255,3 +255,23 @@ def test_copy_visibility_keeps_aliases_and_takes_given_vis():
     z = copy_visibility(b, zero=True)
     assert numpy.all(z["vis"].data == 0) and numpy.all(b["vis"].data == 1)
     assert c.phasecentre is not None and c.attrs is not b.attrs
+
+
+def test_empty_visibilities_need_no_device():
+    """No samples: invert_ng gives a zero image and zero weight sums,
+    predict_ng a zeroed copy, weight_visibility leaves the (empty) weights --
+    what the reference's ducc0 calls and numpy loops give -- before any
+    device work."""
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.imaging import invert_ng, predict_ng, weight_visibility
+    uvw, f, pc, cfg = sim.observation("small-array", ntimes=1, npixel=64)
+    b = sim.make_blockvisibility(uvw[:0], f, pc, cfg)
+    model = sim.model_image(cfg, ([], [], [], [], []), pc, f)
+    model["pixels"].data[...] = 1.0
+    im, sw = invert_ng(b, model)
+    assert numpy.all(im["pixels"].data == 0) and numpy.all(sw == 0)
+    assert im["pixels"].data.shape == model["pixels"].data.shape
+    assert numpy.all(model["pixels"].data == 1.0)
+    p = predict_ng(b, model)
+    assert p is not b and p["vis"].data.shape == b["vis"].data.shape
+    assert weight_visibility(b, model) is b
