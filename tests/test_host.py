@@ -182,8 +182,11 @@ def test_library_exports_every_declared_symbol():
 
 @pytest.mark.parametrize("case", [
     dict(npix_x=63), dict(npol=3), dict(epsilon=1e-8, precision="fp32"),
-    dict(pixsize_x=0.01), dict(sigma=1.9), dict(epsilon=1e-16, precision="fp64")])
+    dict(pixsize_x=0.01), dict(sigma=1.9), dict(epsilon=1e-16, precision="fp64"),
+    dict(nrows=1 << 31, nchan=2)])
 def test_planner_rejects_invalid_arguments(case):
+    """Including more than 2^32 - 1 (row, channel) items in one plan: the
+    item index is 32-bit, so such a call must be split."""
     from rascil_gb300.wgridder import plan_geometry
     kw = dict(npix_x=256, npix_y=256, pixsize_x=1e-3, pixsize_y=1e-3, epsilon=1e-5,
               do_wstacking=True, w_lo=-100.0, w_hi=200.0, precision="fp32", npol=1)
