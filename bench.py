@@ -432,13 +432,15 @@ def cpu_sample(wl, nplanes_sample):
     # scale: all planes, all polarisations (ng.py grids each pol separately)
     t_full = dt * plan.nplanes / len(planes) * wl.npol
     mvis = 2 * wl.nvis / t_full / 1e6
-    desc = ("oracle C gridder (FP64, OpenMP + scipy.fft pocketfft) at sigma %g, W %d (the "
-            "fastest on these cores of %s, estimated s per pol: %s), invert+predict of Stokes I "
-            "over %d of %d w-planes (%d items reach them), time scaled by %d/%d planes x %d "
-            "pols: %.1f s measured"
-            % (sigma, plan.W, "/".join("%g" % x for x in CPU_SIGMAS),
-               ", ".join("%g: %.0f" % kv for kv in sorted(est.items())), len(planes),
-               plan.nplanes, nitems, plan.nplanes, len(planes), wl.npol, dt))
+    why = ("the fastest on these cores of %s, estimated s per pol: %s"
+           % ("/".join("%g" % x for x in CPU_SIGMAS),
+              ", ".join("%g: %.0f" % kv for kv in sorted(est.items())))
+           if est else "the oversampling choice failed; the default")
+    desc = ("oracle C gridder (FP64, OpenMP + scipy.fft pocketfft) at sigma %g, W %d (%s), "
+            "invert+predict of Stokes I over %d of %d w-planes (%d items reach them), time "
+            "scaled by %d/%d planes x %d pols: %.1f s measured"
+            % (sigma, plan.W, why, len(planes), plan.nplanes, nitems, plan.nplanes, len(planes),
+               wl.npol, dt))
     return mvis, cores, desc, dt
 
 
