@@ -4,9 +4,13 @@
 // calculate_blockvisibility_phasor (:1248-1264), as one pass over the
 // visibilities on the GPU.
 //
-//   k_rotate   one thread per (row, channel): d = (u, v, w) . s in
-//              wavelengths, formed and reduced modulo one turn in FP64, then
-//              every pol multiplied by exp(+-2 pi i d).
+//   k_rotate   one thread per (row, channel): d = ((u, v, w) . s) f / c
+//              turns, formed and reduced modulo one turn in FP64, then every
+//              pol multiplied by exp(+-2 pi i d).  The row's dot product is
+//              taken in metres and scaled by the channel's f / c (a shared
+//              table): seven FP64 instructions per (row, channel) instead of
+//              a division and a dozen products -- every warp-level FP64
+//              instruction costs 16 cycles of an SM's FP64 pipe on this part.
 //
 // The imaging path does not call this: invert / predict fuse the same
 // rotation into the plan's per-item factors (gb_plan_params.phase_shift).
@@ -14,20 +18,27 @@
 
 namespace gb {
 
+constexpr int kRotTableChan = 4096;  // channels whose f / c is tabulated per block
+
 template <typename R>
 __global__ void k_rotate(const double *__restrict__ uvw, const double *__restrict__ freq,
                          int64_t nrows, int nchan, int npol, double sl, double sm, double sn,
                          double sign, typename Traits<R>::C *__restrict__ vis) {
+  extern __shared__ double s_k[];
+  const bool table = nchan <= kRotTableChan;
+  if (table) {
+    for (int c = threadIdx.x; c < nchan; c += blockDim.x) s_k[c] = gb_div(freq[c], kSpeedOfLight);
+    __syncthreads();
+  }
   const int64_t n = nrows * nchan;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = i / nchan;
     const int c = (int)(i - r * nchan);
-    const double k = gb_div(freq[c], kSpeedOfLight);
-    const double u = gb_mul(uvw[3 * r], k), v = gb_mul(uvw[3 * r + 1], k),
-                 w = gb_mul(uvw[3 * r + 2], k);
-    double d = gb_add(gb_add(gb_mul(u, sl), gb_mul(v, sm)), gb_mul(w, sn));
-    d = gb_sub(d, rint(d));
+    const double k = table ? s_k[c] : gb_div(freq[c], kSpeedOfLight);
+    const double dm = fma(uvw[3 * r], sl, fma(uvw[3 * r + 1], sm, uvw[3 * r + 2] * sn));
+    double d = dm * k;
+    d -= rint(d);
     R s, co;
     sincos_2pi((R)(sign * d), &s, &co);
     auto *x = vis + i * npol;
@@ -76,13 +87,15 @@ extern "C" int gb_phase_rotate(const double *uvw_dev, const double *freq_dev, in
   const double sign = inverse ? -1.0 : 1.0;
   const double cb = precision == GB_FP64 ? 16.0 : 8.0;
   ProfScope ps(kProfRotate, s, 2.0 * cb * (double)n * npol + 24.0 * nrows);
+  const size_t smem = nchan <= kRotTableChan ? sizeof(double) * (size_t)nchan : 0;
   if (precision == GB_FP64)
-    k_rotate<double><<<blocks, kThreads, 0, s>>>(uvw_dev, freq_dev, nrows, nchan, npol, s_l,
-                                                 s_m, s_n, sign,
-                                                 reinterpret_cast<double2 *>(vis_dev));
+    k_rotate<double><<<blocks, kThreads, smem, s>>>(uvw_dev, freq_dev, nrows, nchan, npol, s_l,
+                                                    s_m, s_n, sign,
+                                                    reinterpret_cast<double2 *>(vis_dev));
   else
-    k_rotate<float><<<blocks, kThreads, 0, s>>>(uvw_dev, freq_dev, nrows, nchan, npol, s_l, s_m,
-                                                s_n, sign, reinterpret_cast<float2 *>(vis_dev));
+    k_rotate<float><<<blocks, kThreads, smem, s>>>(uvw_dev, freq_dev, nrows, nchan, npol, s_l,
+                                                   s_m, s_n, sign,
+                                                   reinterpret_cast<float2 *>(vis_dev));
   GB_LAUNCH_CHECK("k_rotate");
   return GB_OK;
 }
