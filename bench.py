@@ -83,13 +83,26 @@ def parse():
     ap.add_argument("--fft-mode", default="auto", choices=["auto", "columns", "cufft2d"],
                     help="per-plane transforms of the FP32 form (auto: column kernels where "
                          "they apply)")
+    ap.add_argument("--no-mid", action="store_true",
+                    help="skip the MID-like configuration's rate and accuracy")
+    ap.add_argument("--mid-steps", type=int, default=2)
+    ap.add_argument("--mid-warmup", type=int, default=1)
+    ap.add_argument("--no-reduced", action="store_true",
+                    help="skip the reduced-case accuracy of every form (GPU and CPU)")
     ap.add_argument("--json-out", default=None)
     ap.add_argument("--path", default="imaging",
-                    choices=["imaging", "weights", "rotation", "lists"],
+                    choices=["imaging", "weights", "rotation", "lists", "batch", "autograd",
+                             "dft"],
                     help="imaging: the headline invert+predict step (default); weights: "
                          "imaging weights; rotation: the phase rotation (standalone kernel and "
                          "its cost fused into the imaging step); lists: the list workflows on "
-                         "256 uneven snapshots")
+                         "256 uneven snapshots; batch: the 256 uneven snapshots as one batched "
+                         "device program; autograd: 200 gradient-descent steps of the "
+                         "differentiable predict; dft: the component DFT against the "
+                         "reference's own CUDA kernel")
+    ap.add_argument("--gd-steps", type=int, default=200)
+    ap.add_argument("--nsnap", type=int, default=256)
+    ap.add_argument("--e2e-gd-steps", type=int, default=20)
     return ap.parse_args()
 
 
@@ -157,9 +170,11 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # workload
 
-class Workload:
-    def __init__(self, name, scale, device):
-        import torch
+class CpuWorkload:
+    """The workload's geometry, sources and model image on the host (numpy
+    only): everything the CPU legs need, built without the GPU library."""
+
+    def __init__(self, name, scale):
         from rascil_gb300 import simulation as sim
         from rascil_gb300.polarisation import conversion_matrix, PolarisationFrame
 
@@ -184,19 +199,42 @@ class Workload:
         self.pm_in = conversion_matrix(self.vis_pol, self.img_pol)
         self.pm_out = conversion_matrix(self.img_pol, self.vis_pol)
         self.src = sim.sources(cfg, seed=0)
-        self.device = device
-        # device copies: uvw as ng.py hands it to the gridder (u, w flipped)
-        u = torch.from_numpy(uvw.reshape(-1, 3).copy()).to(device)
-        self.uvw_raw = u.clone()
-        u[:, 0].neg_()
-        u[:, 2].neg_()
-        self.uvw = u
-        self.freq_dev = torch.from_numpy(freq.copy()).to(device)
         # model image (Stokes I of the sources at their pixels), [pol][y][x]
         model = numpy.zeros((self.npol, self.npixel, self.npixel), dtype=numpy.float32)
         ix, iy, l, m, flux = self.src
         numpy.add.at(model[0], (iy, ix), flux)
-        self.model32 = torch.from_numpy(model).to(device)
+        self.model_host = model
+
+    def flipped_uvw(self):
+        """uvw [nrows, 3] as ng.py hands them to the gridder (u, w negated)."""
+        u = self.uvw_host.reshape(-1, 3).copy()
+        u[:, 0] *= -1.0
+        u[:, 2] *= -1.0
+        return u
+
+
+class Workload:
+    """The workload on the device: uvw, frequencies, the model image and the
+    sources' visibilities (GPU component DFT) plus noise."""
+
+    def __init__(self, name, scale, device, cpu=None):
+        import torch
+        cw = cpu or CpuWorkload(name, scale)
+        for k in ("name", "scale", "cfg", "uvw_host", "freq", "phasecentre", "ntimes", "nbl",
+                  "nrows", "nchan", "vis_pol", "img_pol", "npv", "npol", "npixel", "cell",
+                  "epsilon", "nvis", "pm_in", "pm_out", "src"):
+            setattr(self, k, getattr(cw, k))
+        cfg = self.cfg
+        from rascil_gb300 import simulation as sim
+        self.device = device
+        # device copies: uvw as ng.py hands it to the gridder (u, w flipped)
+        u = torch.from_numpy(self.uvw_host.reshape(-1, 3).copy()).to(device)
+        self.uvw_raw = u.clone()
+        u[:, 0].neg_()
+        u[:, 2].neg_()
+        self.uvw = u
+        self.freq_dev = torch.from_numpy(self.freq.copy()).to(device)
+        self.model32 = torch.from_numpy(cw.model_host).to(device)
         # visibilities of the sources (component DFT) plus noise, vis frame
         from rascil_gb300.dft import dft_components
         lmn = sim.lmn_rows(self.src)
@@ -310,7 +348,23 @@ def accuracy(wl, dirty, pred, precision, nrows_check=512, npix_check=192):
                                                          min(npix_check, len(ix)), npix_check)}
 
 
-def roofline(stats, peaks):
+def _ncu_traffic(kernel):
+    """profiles/ncu_traffic.json: per kernel, the DRAM bytes ncu measured per
+    launch over the algorithmic bytes this bench counts for the same launches
+    (captured on a smaller case of the same kernel)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError, AttributeError):
+        return None
+
+
+# update-rate rooflines: shared-memory instructions per (item, pol, cell) update
+UPDATE_COST = {"k_grid": ("atomics", 2.0, "2 conflict-free 32-bit shared atomic adds (re, im)"),
+               "k_degrid": ("loads", 1.0, "1 conflict-free 8-byte shared load (complex64)")}
+
+
+def roofline(stats, peaks, smem=None):
     mine = {k: v for k, v in stats.items() if not k.startswith("cufft")}
     total_ms = sum(v["ms"] for v in stats.values())
     dom = max(mine, key=lambda k: mine[k]["ms"])
@@ -319,23 +373,40 @@ def roofline(stats, peaks):
     peak = peaks.get("hbm_gbs")
     src = "of measured" if peak else "of fallback"
     peak = peak or 6800.0
+    bpl = d["bytes"] / d["launches"]
+    t = _ncu_traffic(dom)
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            with open(tpath) as f:
-                t = json.load(f)
-            traffic = t.get(dom)
-        except (OSError, ValueError):
-            traffic = None
+    if t and t.get("dram_over_algorithmic"):
+        traffic = round(t["dram_over_algorithmic"] * bpl, 1)
     kernels = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
                    "share": round(v["ms"] / total_ms, 4) if total_ms else None,
+                   "bytes": v["bytes"],
                    "gbs": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] else None}
                for k, v in sorted(stats.items(), key=lambda kv: -kv[1]["ms"])}
-    return ({"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak,
-             "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": src,
-             "bytes_per_launch": d["bytes"] / d["launches"],
-             "ms_per_launch": d["ms"] / d["launches"], "traffic": traffic}, kernels)
+    secondary = {}
+    for k, (what, per, desc) in UPDATE_COST.items():
+        v = stats.get(k)
+        if not v or not v.get("updates") or not v["ms"]:
+            continue
+        ups = v["updates"] / (v["ms"] * 1e-3)
+        kernels[k]["updates_per_s"] = ups
+        entry = {"updates_per_s": ups, "cost": desc}
+        if smem:
+            pk = (smem[0] if what == "atomics" else smem[1]) / per
+            entry.update({"peak_updates_per_s": pk, "frac": round(ups / pk, 4),
+                          "peak_source": "measured shared-memory %s rate of this GPU "
+                                         "(gb_probe_smem_peaks)" % what})
+        secondary[k] = entry
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": src,
+            "bytes_per_launch": bpl, "ms_per_launch": d["ms"] / d["launches"],
+            "traffic": traffic,
+            "traffic_basis": (None if traffic is None else
+                              "ncu dram__bytes_read+write / algorithmic bytes = %.3f on %s, "
+                              "times this launch's algorithmic bytes"
+                              % (t["dram_over_algorithmic"], t.get("case", "?"))),
+            "secondary": secondary}
+    return roof, kernels
 
 
 # ---------------------------------------------------------------------------
@@ -398,50 +469,143 @@ def cpu_choose_sigma(u, v, w, npix, cell, eps, cores, nplanes_probe=2, sigmas=CP
     return min(est, key=est.get), est
 
 
-def cpu_sample(wl, nplanes_sample):
+def cpu_sample(cw, nplanes_sample):
     """Invert + predict of the full workload restricted to an evenly spread
     subset of w-planes, one polarisation, FP64 on all host cores, at the
-    oversampling fastest on the CPU; returns (extrapolated Mvis/s, cores,
-    description, measured seconds)."""
-    import torch
+    oversampling fastest on the CPU.  Host only (``cw`` is a CpuWorkload):
+    the sampled items' values are seeded complex Gaussians (the gridder's
+    time does not depend on them).  Returns a dict: the extrapolated Mvis/s,
+    cores, description, measured seconds, the full-step estimate and the
+    oversampling used."""
     from oracle import cgridder
-    s = wl.freq / 299792458.0
-    uvw = wl.uvw.cpu().numpy()  # flipped, as ng.py passes to ducc0
+    s = cw.freq / 299792458.0
+    uvw = cw.flipped_uvw()  # as ng.py passes to ducc0
     u = (uvw[:, 0:1] * s).ravel()
     v = (uvw[:, 1:2] * s).ravel()
     w = (uvw[:, 2:3] * s).ravel()
     cores = cgridder.max_threads()
-    key = (wl.name, wl.scale)
+    key = (cw.name, cw.scale)
     if key not in _CPU_SIGMA:
         try:
-            _CPU_SIGMA[key] = cpu_choose_sigma(u, v, w, wl.npixel, wl.cell, wl.epsilon, cores)
-        except Exception as e:  # the choice is an optimisation: keep the measured default
+            _CPU_SIGMA[key] = cpu_choose_sigma(u, v, w, cw.npixel, cw.cell, cw.epsilon, cores)
+        except (ValueError, IndexError, OSError) as e:  # an optimisation: keep the default
             print("cpu_choose_sigma failed (%s); the CPU baseline uses sigma 2" % e,
                   file=sys.stderr)
             _CPU_SIGMA[key] = (2.0, {})
     sigma, est = _CPU_SIGMA[key]
-    m = torch.from_numpy(wl.pm_in[0]).to(wl.device)
 
-    def values(idx):  # Stokes I of the chosen items, formed on the device
-        vi = wl.vis32.to(torch.complex128) @ m
-        return vi.reshape(-1)[torch.from_numpy(idx).to(wl.device)].cpu().numpy()
+    def values(idx):
+        rng = numpy.random.default_rng(11)
+        return rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
 
-    model = wl.model32[0].double().cpu().numpy()
-    dt, plan, planes, nitems = cpu_gridder_sample(u, v, w, values, model, wl.npixel, wl.cell,
-                                                  wl.epsilon, nplanes_sample, sigma, cores)
+    model = cw.model_host[0].astype(numpy.float64)
+    dt, plan, planes, nitems = cpu_gridder_sample(u, v, w, values, model, cw.npixel, cw.cell,
+                                                  cw.epsilon, nplanes_sample, sigma, cores)
     # scale: all planes, all polarisations (ng.py grids each pol separately)
-    t_full = dt * plan.nplanes / len(planes) * wl.npol
-    mvis = 2 * wl.nvis / t_full / 1e6
+    scale = plan.nplanes / len(planes) * cw.npol
+    t_full = dt * scale
+    mvis = 2 * cw.nvis / t_full / 1e6
     why = ("the fastest on these cores of %s, estimated s per pol: %s"
            % ("/".join("%g" % x for x in CPU_SIGMAS),
               ", ".join("%g: %.0f" % kv for kv in sorted(est.items())))
            if est else "the oversampling choice failed; the default")
     desc = ("oracle C gridder (FP64, OpenMP + scipy.fft pocketfft) at sigma %g, W %d (%s), "
-            "invert+predict of Stokes I over %d of %d w-planes (%d items reach them), time "
-            "scaled by %d/%d planes x %d pols: %.1f s measured"
+            "invert+predict of one polarisation over %d of %d w-planes (%d items reach them; "
+            "seeded Gaussian values), time scaled by %d/%d planes x %d pols: %.2f s measured"
             % (sigma, plan.W, why, len(planes), plan.nplanes, nitems, plan.nplanes, len(planes),
-               wl.npol, dt))
-    return mvis, cores, desc, dt
+               cw.npol, dt))
+    return {"mvis": mvis, "cores": cores, "desc": desc, "sample_s": dt, "full_s": t_full,
+            "scale": scale, "sigma": sigma, "W": plan.W, "planes": len(planes),
+            "nplanes": plan.nplanes}
+
+
+# The reduced case on which both arms state their error against the exact
+# DFT at the same epsilon: the workload's geometry (every baseline, its
+# frequency band), 2 times x 4 channels, a 1024^2 image at the configured
+# cell, Stokes I of its first 64 sources.
+REDUCED = dict(ntimes=2, nchan=4, npixel=1024, nsrc=64, npix_check=128, nrows_check=256)
+
+
+def reduced_case(name):
+    """Host arrays of the reduced accuracy case: flipped uvw, freq, Stokes I
+    visibilities [nrows, nchan] (exact FP64 component DFT, the oracle), the
+    model image [y][x], the sampled pixels and rows with their exact
+    invert / predict values (oracle direct sums)."""
+    from oracle import dft as odft
+    from rascil_gb300 import simulation as sim
+    uvw, freq, pc, cfg = sim.observation(name, seed=0, ntimes=REDUCED["ntimes"],
+                                         nchan=REDUCED["nchan"], npixel=REDUCED["npixel"])
+    cfg = dict(cfg, nsrc=REDUCED["nsrc"])
+    ix, iy, l, m, flux = sim.sources(cfg, seed=0)
+    n = numpy.sqrt(1.0 - l * l - m * m)
+    lmn = numpy.stack([l, m, n - 1.0], -1)
+    uvw_lambda = uvw[:, :, None, :] * (freq / odft.SPEED_OF_LIGHT)[None, None, :, None]
+    vis = odft.dft_cpu_looped(lmn, uvw_lambda, (flux / n)[:, None, None] *
+                              numpy.ones((1, len(freq), 1)))[..., 0]
+    vis = vis.reshape(-1, len(freq))
+    npix, cell = cfg["npixel"], cfg["cellsize"]
+    model = numpy.zeros((npix, npix))
+    numpy.add.at(model, (iy, ix), flux)
+    fu = uvw.reshape(-1, 3) * numpy.array([-1.0, 1.0, -1.0])
+    rng = numpy.random.default_rng(5)
+    k = REDUCED["npix_check"] // 2
+    pix = numpy.concatenate([numpy.stack([ix, iy], -1)[:k], rng.integers(0, npix, (k, 2))])
+    truth_px = odft.ms2dirty_dft(fu, freq, vis, None, npix, npix, cell, cell, True,
+                                 pixel_subset=(pix[:, 0], pix[:, 1]), chunk=16)
+    rows = numpy.sort(rng.choice(fu.shape[0], REDUCED["nrows_check"], replace=False))
+    truth_v = odft.dirty2ms_dft(fu, freq, model.T, None, cell, cell, True, row_subset=rows)
+    return dict(uvw=fu, freq=freq, vis=vis, model=model, npix=npix, cell=cell,
+                eps=cfg["epsilon"], pix=pix, truth_px=truth_px, rows=rows, truth_v=truth_v,
+                desc="%s geometry, %d times x %d baselines x %d chan, %d^2 image (cell %g), "
+                     "Stokes I of %d sources; invert at %d pixels, predict at %d rows x %d "
+                     "chan, against the oracle's FP64 direct sums"
+                     % (name, uvw.shape[0], uvw.shape[1], len(freq), npix, cell, len(flux),
+                        len(pix), len(rows), len(freq)))
+
+
+def _rel(a, b):
+    a, b = numpy.asarray(a), numpy.asarray(b)
+    return float(numpy.linalg.norm((a - b).ravel()) / numpy.linalg.norm(b.ravel()))
+
+
+def cpu_accuracy(rc, sigma, cores):
+    """The CPU path's own error on the reduced case at the same epsilon: the
+    oracle's C gridder (FP64, every w-plane) at the CPU's oversampling."""
+    from oracle import cgridder
+    dirty = cgridder.ms2dirty(rc["uvw"], rc["freq"], rc["vis"], None, rc["npix"], rc["npix"],
+                              rc["cell"], rc["cell"], rc["eps"], True, nthreads=cores,
+                              sigma=sigma)
+    got_px = dirty[rc["pix"][:, 0], rc["pix"][:, 1]]
+    pred = cgridder.dirty2ms(rc["uvw"][rc["rows"]], rc["freq"], rc["model"].T, None, rc["cell"],
+                             rc["cell"], rc["eps"], True, nthreads=cores, sigma=sigma)
+    return {"invert_rel_rms": _rel(got_px, rc["truth_px"]),
+            "predict_rel_rms": _rel(pred, rc["truth_v"]),
+            "form": "oracle C gridder FP64, sigma %g" % sigma}
+
+
+def gpu_accuracy(rc, precision, device):
+    """The GPU forms' error on the reduced case (Plan: invert + predict)."""
+    import torch
+    from rascil_gb300.wgridder import Plan
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    rdt = torch.float64 if precision == "fp64" else torch.float32
+    u = torch.from_numpy(rc["uvw"]).to(device)
+    f = torch.from_numpy(rc["freq"].copy()).to(device)
+    plan = Plan(u, f, rc["npix"], rc["npix"], rc["cell"], rc["cell"], rc["eps"], True, npol=1,
+                precision=precision)
+    try:
+        vis = torch.from_numpy(rc["vis"]).to(device=device, dtype=cdt).reshape(plan.nrows,
+                                                                             plan.nchan, 1)
+        dirty = plan.ms2dirty(vis, layout="xy")[0].double().cpu().numpy()
+        model = torch.from_numpy(rc["model"].T.copy()).to(device=device, dtype=rdt)
+        pred = plan.dirty2ms(model.reshape(1, rc["npix"], rc["npix"]), layout="xy")
+        pred = pred[torch.from_numpy(rc["rows"]).to(device), :, 0].to(torch.complex128)
+        info = plan.info
+    finally:
+        plan.close()
+    return {"invert_rel_rms": _rel(dirty[rc["pix"][:, 0], rc["pix"][:, 1]], rc["truth_px"]),
+            "predict_rel_rms": _rel(pred.cpu().numpy(), rc["truth_v"]),
+            "form": "%s, sigma %g, W %d" % (precision, info["sigma"], info["support"])}
 
 
 # ---------------------------------------------------------------------------
@@ -849,7 +1013,352 @@ def _ptr_stream(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
-AUX_PATHS = {"weights": bench_weights, "rotation": bench_rotation, "lists": bench_lists}
+def _blob_sky(npix, cell, nsrc, nblob, seed):
+    """The differentiable-predict sky: ``nsrc`` point sources U[0.01, 1] Jy at
+    pixel centres plus ``nblob`` circular Gaussian blobs (sigma 3-10 px,
+    peak U[0.01, 1] Jy, cut at 4 sigma), [y][x] float64, within the inner
+    half of the image."""
+    rng = numpy.random.default_rng(seed)
+    sky = numpy.zeros((npix, npix))
+    lo, hi = npix // 4, 3 * npix // 4
+    ix = rng.integers(lo, hi, nsrc)
+    iy = rng.integers(lo, hi, nsrc)
+    numpy.add.at(sky, (iy, ix), rng.uniform(0.01, 1.0, nsrc))
+    for _ in range(nblob):
+        sg = rng.uniform(3.0, 10.0)
+        cx, cy = rng.integers(lo, hi, 2)
+        r = int(4 * sg)
+        yy, xx = numpy.mgrid[cy - r:cy + r + 1, cx - r:cx + r + 1]
+        amp = rng.uniform(0.01, 1.0)
+        sky[cy - r:cy + r + 1, cx - r:cx + r + 1] += amp * numpy.exp(
+            -((xx - cx) ** 2 + (yy - cy) ** 2) / (2 * sg * sg))
+    return sky
+
+
+def bench_autograd(args):
+    """The differentiable predict at its stated size: a 2048^2 FP32 sky
+    (200 points + 20 Gaussian blobs), 128 antennas in a 1 km disk, 8
+    channels over 150-158 MHz, 64 times, Stokes I, per-antenna per-channel
+    gains (amplitude 1 + N(0, 0.05), phase U(-pi/8, pi/8)) applied as
+    g_i conj(g_j); loss sum |V_pred - V_obs|^2 with V_obs from the FP64
+    DFT of the sky under the true gains.  Timed: 200 gradient-descent steps
+    on the image and the gains (forward dirty2ms + gains, backward = the
+    gridder + the gain-gradient kernel), one plan for the run."""
+    import torch
+    from rascil_gb300 import _lib
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.autograd import apply_gains, baseline_antennas, predict
+    from rascil_gb300.dft import dft_components
+    from rascil_gb300.wgridder import Plan
+    device = torch.device("cuda", torch.cuda.current_device())
+    _lib.load()
+    uvw, freq, pc, cfg = sim.observation("gain-solve", seed=0)
+    nt, nbl, _ = uvw.shape
+    nants = int(round((1 + numpy.sqrt(1 + 8 * nbl)) / 2))
+    npix, cell, eps = cfg["npixel"], cfg["cellsize"], cfg["epsilon"]
+    R, C = nt * nbl, len(freq)
+    nvis = R * C
+    sky = _blob_sky(npix, cell, 200, 20, seed=4)
+    raw = torch.from_numpy(uvw.reshape(-1, 3).copy()).to(device)
+    fu = raw.clone()
+    fu[:, 0].neg_()
+    fu[:, 2].neg_()
+    f = torch.from_numpy(freq.copy()).to(device)
+    # V_obs: FP64 DFT over every nonzero sky pixel (flux / n at its l, m),
+    # the exact image-plane operator, then the true gains
+    iy, ix = numpy.nonzero(sky)
+    l = -(ix - npix // 2) * cell
+    m = (iy - npix // 2) * cell
+    n = numpy.sqrt(1.0 - l * l - m * m)
+    lmn = numpy.stack([l, m, n - 1.0], -1)
+    flux = (sky[iy, ix] / n)[:, None, None] * numpy.ones((1, C, 1))
+    t0 = time.perf_counter()
+    v_true = dft_components(raw, f, lmn, flux, precision="fp64", exact=True)
+    torch.cuda.synchronize()
+    t_dft = time.perf_counter() - t0
+    rng = numpy.random.default_rng(9)
+    g_true = (1 + 0.05 * rng.normal(size=(nants, C))) * numpy.exp(
+        1j * rng.uniform(-numpy.pi / 8, numpy.pi / 8, (nants, C)))
+    a1, a2 = baseline_antennas(nants, nt, device)
+    gt = torch.from_numpy(g_true).to(device)
+    obs = apply_gains(v_true, gt, a1, a2).to(torch.complex64).contiguous()
+    del v_true
+    plan = Plan(fu, f, npix, npix, cell, cell, eps, True, npol=1, precision="fp32")
+    # steepest-descent step sizes: the image's Hessian peak is 2 nvis (unit
+    # weights, gains near 1); the gains' is 2 sum over an antenna's rows of |V|^2
+    lr_x = 0.5 / nvis
+    vis_pow = float(obs.abs().pow(2).mean())
+    lr_g = 0.25 / ((nants - 1) * nt * max(vis_pow, 1e-30))
+
+    def gd_run(nsteps, x, g, host_obs=None):
+        losses = []
+        for _ in range(nsteps):
+            o = obs
+            if host_obs is not None:
+                o = host_obs.to(device, non_blocking=True)
+            x.grad = None
+            g.grad = None
+            loss = (apply_gains(predict(x, plan), g, a1, a2) - o).abs().pow(2).sum()
+            loss.backward()
+            with torch.no_grad():
+                x -= lr_x * x.grad
+                g -= lr_g * g.grad
+            losses.append(loss.detach())
+        return losses
+
+    def fresh():
+        x = torch.zeros((1, npix, npix), dtype=torch.float32, device=device, requires_grad=True)
+        g = torch.ones((nants, C), dtype=torch.complex128, device=device, requires_grad=True)
+        return x, g
+
+    x, g = fresh()
+    gd_run(args.warmup, x, g)  # warm-up (plan caches, cuFFT)
+    x, g = fresh()
+    sampler = ClockSampler(device.index)
+    _lib.profile_reset()
+    _lib.profile_enable(True)
+    sampler.start()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    losses = gd_run(args.gd_steps, x, g)
+    b.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    _lib.profile_enable(False)
+    stats = _lib.profile_read()
+    ms = a.elapsed_time(b) / args.gd_steps
+    losses = [float(v) for v in losses]
+    img_err = float(numpy.linalg.norm(x.detach()[0].double().cpu().numpy() - sky) /
+                    numpy.linalg.norm(sky))
+    roof, kernels = roofline(stats, load_peaks())
+    launches = sum(v["launches"] for k, v in stats.items() if not k.startswith("cufft"))
+    # checks at this size: the dot-product identity through the Function
+    xr = torch.randn((1, npix, npix), device=device, dtype=torch.float32, requires_grad=True)
+    yr = torch.view_as_complex(torch.randn((R, C, 1, 2), device=device)).contiguous()
+    vr = predict(xr, plan)
+    lhs = torch.real(torch.vdot(yr.reshape(-1).to(torch.complex128),
+                                vr.reshape(-1).to(torch.complex128)))
+    lhs.backward()
+    rhs = (xr.detach().double() * xr.grad.double()).sum()
+    dot = abs(float(lhs) - float(rhs)) / float(
+        torch.linalg.vector_norm(vr.detach().to(torch.complex128)) *
+        torch.linalg.vector_norm(yr.to(torch.complex128)))
+    # end to end: V_obs copied from page-locked host memory each step, loss read back
+    host_obs = torch.empty(obs.shape, dtype=obs.dtype, pin_memory=True)
+    host_obs.copy_(obs)
+    x2, g2 = fresh()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ls = gd_run(args.e2e_gd_steps, x2, g2, host_obs)
+    [float(v) for v in ls]
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_gd_steps
+    # CPU baseline: one gradient step's dirty2ms + ms2dirty on the oracle's C
+    # gridder, sampled over w-planes and scaled (host only)
+    from oracle import cgridder
+    cores = cgridder.max_threads()
+    fun = uvw.reshape(-1, 3) * numpy.array([-1.0, 1.0, -1.0])
+    s_ = freq / 299792458.0
+    uu, vv, ww = [(fun[:, i:i + 1] * s_).ravel() for i in range(3)]
+    rng2 = numpy.random.default_rng(2)
+    dt, cplan, planes, nitems = cpu_gridder_sample(
+        uu, vv, ww, lambda idx: rng2.standard_normal(idx.size) + 1j * rng2.standard_normal(
+            idx.size), sky, npix, cell, eps, args.cpu_planes, 2.0, cores)
+    t_cpu = dt * cplan.nplanes / len(planes)
+    plan.close()
+    workload = {"workload": "differentiable predict: %d^2 FP32 sky (200 points + 20 Gaussian "
+                            "blobs), %d antennas (%d baselines) x %d times, %d chan %.0f-%.0f "
+                            "MHz, Stokes I, per-antenna gains, eps %g, %d GD steps"
+                            % (npix, nants, nbl, nt, C, freq[0] / 1e6, freq[-1] / 1e6, eps,
+                               args.gd_steps),
+                "nvis": nvis, "l2": "plane batches and visibilities larger than L2"}
+    step_vis = 2 * nvis  # one predict forward + one gridder backward per step
+    return _aux_line(args, "Mvis/s gradient-descent steps (predict forward + adjoint backward) "
+                     "on 1 GB300", step_vis / (ms * 1e-3) / 1e6, "Mvis/s", ms, workload, roof,
+                     kernels, clocks, int(launches / args.gd_steps), dtype="f32",
+                     steps=args.gd_steps,
+                     gd={"steps": args.gd_steps, "ms_per_step": round(ms, 3),
+                         "loss_first": losses[0], "loss_last": losses[-1],
+                         "image_rel_err_last": img_err,
+                         "obs_dft_s": round(t_dft, 2), "obs_components": int(len(ix))},
+                     checks={"dot_product_rel_to_cauchy_schwarz": dot},
+                     cpu_baseline={"value": round(step_vis / t_cpu / 1e6, 4), "unit": "Mvis/s",
+                                   "cores": cores, "kind": "port",
+                                   "sample": "oracle C gridder (FP64), dirty2ms + ms2dirty of "
+                                             "one step over %d of %d w-planes (%d items), "
+                                             "scaled: %.2f s measured"
+                                             % (len(planes), cplan.nplanes, nitems, dt)},
+                     e2e={"value": round(step_vis / e2e_s / 1e6, 3), "unit": "Mvis/s",
+                          "h2d_bytes_per_step": int(obs.numel() * 8), "d2h_bytes_per_step": 8,
+                          "s_per_step": round(e2e_s, 4), "steps": args.e2e_gd_steps,
+                          "api": "rascil_gb300.autograd.predict + apply_gains, torch autograd; "
+                                 "V_obs from page-locked host memory each step, loss read back"})
+
+
+def bench_dft(args):
+    """The component DFT (dft_skycomponent_visibility) against the
+    reference's own CUDA DFT kernel on the same GPU and inputs: LOW-like
+    geometry, 2 hour angles x 130,816 baselines x 16 channels x 4 linear
+    pols, 1,000 components, FP64 in both.  The reference kernel is the
+    source string of rascil/processing_components/imaging/dft.py:181-258,
+    built by oracle/ref_dft (its timing is this path's reference arm)."""
+    import torch
+    from rascil_gb300 import _lib
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.dft import dft_components
+    device = torch.device("cuda", torch.cuda.current_device())
+    _lib.load()
+    uvw, freq, pc, cfg = sim.observation("low-like", ntimes=2)
+    src = sim.sources(cfg)
+    lmn = sim.lmn_rows(src)
+    flux = sim.component_fluxes(cfg, src, len(freq))
+    u = torch.from_numpy(uvw.reshape(-1, 3).copy()).to(device)
+    f = torch.from_numpy(freq.copy()).to(device)
+    nvis = uvw.shape[0] * uvw.shape[1] * len(freq) * flux.shape[-1]
+    sampler = ClockSampler(device.index)
+    ms, clocks, stats = _event_loop(
+        lambda: dft_components(u, f, lmn, flux, precision="fp64", exact=True), args.steps,
+        args.warmup, sampler)
+    ms_fast, _, _ = _event_loop(
+        lambda: dft_components(u, f, lmn, flux, precision="fp32", exact=False), args.steps,
+        args.warmup, profile=False)
+    ours = dft_components(u, f, lmn, flux, precision="fp64", exact=True).cpu().numpy()
+    ref_line = {"unavailable": "the reference kernel was not built (oracle/ref_dft)"}
+    try:
+        from oracle import ref_dft
+        uvw_lambda = (torch.from_numpy(uvw).to(device)[:, :, None, :]
+                      * (f / 299792458.0)[None, None, :, None]).contiguous()
+        lmn_t = torch.from_numpy(lmn).to(device).contiguous()
+        flux_t = torch.from_numpy(flux).to(device).contiguous()
+        ref = torch.zeros(uvw.shape[:2] + (len(freq), flux.shape[-1]), dtype=torch.complex128,
+                          device=device)
+        ms_ref, _, _ = _event_loop(lambda: ref_dft.run(lmn_t, flux_t, uvw_lambda, ref),
+                                   args.steps, args.warmup, profile=False)
+        b_ = ref.cpu().numpy().reshape(ours.shape)
+        ref_line = {"value": round(nvis / (ms_ref * 1e-3) / 1e6, 3), "unit": "Mvis/s",
+                    "ms": round(ms_ref, 3), "speedup_exact": round(ms_ref / ms, 3),
+                    "speedup_fast": round(ms_ref / ms_fast, 3),
+                    "max_rel_diff_exact": float(numpy.max(numpy.abs(ours - b_)) /
+                                                numpy.max(numpy.abs(b_))),
+                    "kind": "the reference's own CUDA dft_kernel (dft.py:181-258), same GPU"}
+    except (ImportError, OSError, RuntimeError) as e:
+        ref_line = {"unavailable": str(e)}
+    # CPU baseline: the oracle's looped DFT (dft_cpu_looped restated) on the
+    # first rows
+    from oracle import dft as odft
+    rs = 256
+    ul = uvw.reshape(-1, 3)[:rs][None, :, None, :] * (freq / odft.SPEED_OF_LIGHT)[None, None, :,
+                                                                                   None]
+    t0 = time.perf_counter()
+    odft.dft_cpu_looped(lmn, ul, flux)
+    cpu_dt = time.perf_counter() - t0
+    roof, kernels = roofline(stats, load_peaks())
+    workload = {"workload": "component DFT: LOW-like geometry, 2 times x %d baselines x %d chan "
+                            "x %d pols, %d components, FP64" % (uvw.shape[1], len(freq),
+                                                               flux.shape[-1], len(lmn)),
+                "nvis": nvis, "components": len(lmn)}
+    return _aux_line(args, "Mvis/s component DFT (FP64, 1000 components) on 1 GB300",
+                     nvis / (ms * 1e-3) / 1e6, "Mvis/s", ms, workload, roof, kernels, clocks, 1,
+                     dtype="f64", fast_form={"ms": round(ms_fast, 3),
+                                             "value": round(nvis / (ms_fast * 1e-3) / 1e6, 3)},
+                     reference_kernel=ref_line,
+                     cpu_baseline={"value": round(rs * len(freq) * flux.shape[-1] / cpu_dt / 1e6,
+                                                  4), "unit": "Mvis/s", "cores": 1,
+                                   "kind": "port", "sample": "oracle dft_cpu_looped (numpy) on "
+                                   "the first %d rows: %.2f s" % (rs, cpu_dt)},
+                     e2e=None)
+
+
+def bench_batch(args):
+    """The batched configuration: 256 independent snapshots (32-512 antennas
+    in a 1 km disk, 1-8 channels in 100-200 MHz, 1-16 hour angles, 5e3-2e6
+    Stokes I complex64 visibilities each, image side 256-2048, cell 1/(2.2
+    max|uv|), epsilon 1e-5), invert + predict of every snapshot on device
+    buffers.  Timed with CUDA events: the batch as one device program
+    (SnapshotBatch), against one plan and call sequence per snapshot on one
+    stream (plan creation included in both); the CPU oracle on a sample of
+    snapshots, scaled by visibility count."""
+    import torch
+    from rascil_gb300 import _lib
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.batch import SnapshotBatch
+    from rascil_gb300.wgridder import Plan
+    device = torch.device("cuda", torch.cuda.current_device())
+    _lib.load()
+    raw = sim.snapshot_batch(args.nsnap)
+    g = torch.Generator(device=device)
+    g.manual_seed(1)
+    snaps, vis, models = [], [], []
+    for r in raw:
+        u = torch.from_numpy(r["uvw"].reshape(-1, 3) * numpy.array([-1.0, 1.0, -1.0])).to(device)
+        f = torch.from_numpy(r["freq"].copy()).to(device)
+        snaps.append(dict(uvw=u, freq=f, npix=r["npix"], cell=r["cell"]))
+        shape = (u.shape[0], f.shape[0], 1, 2)
+        vis.append(torch.view_as_complex(torch.randn(shape, generator=g, device=device))
+                   .contiguous())
+        m = torch.zeros((1, r["npix"], r["npix"]), device=device)
+        m[0, r["npix"] // 2, r["npix"] // 2 + 3] = 1.0
+        models.append(m)
+    nvis = sum(r["nvis"] for r in raw)
+    eps = 1e-5
+
+    def one_by_one():
+        for i, sn in enumerate(snaps):
+            p = Plan(sn["uvw"], sn["freq"], sn["npix"], sn["npix"], sn["cell"], sn["cell"], eps,
+                     True, precision="fp32", grid_budget_bytes=2 << 30)
+            p.ms2dirty(vis[i], layout="yx")
+            p.dirty2ms(models[i], layout="yx")
+            p.close()
+
+    def batched():
+        b = SnapshotBatch(snaps, eps, precision="fp32", nslots=8)
+        b.run(vis, models)
+        b.close()
+
+    sampler = ClockSampler(device.index)
+    ms_batch, clocks, stats = _event_loop(batched, args.steps, args.warmup, sampler)
+    ms_seq, _, _ = _event_loop(one_by_one, 1, 1, profile=False)
+    launches = sum(v["launches"] for k, v in stats.items() if not k.startswith("cufft"))
+    roof, kernels = roofline(stats, load_peaks())
+    # CPU baseline: the oracle's C gridder on a sample of snapshots (host only)
+    from oracle import cgridder
+    rng = numpy.random.default_rng(1)
+    idx = rng.choice(len(raw), size=min(6, len(raw)), replace=False)
+    cpu_t, cpu_v = 0.0, 0
+    for i in idx:
+        r = raw[i]
+        uvw = r["uvw"].reshape(-1, 3) * numpy.array([-1.0, 1.0, -1.0])
+        ms_ = rng.standard_normal((uvw.shape[0], len(r["freq"]))) * (1 + 0j)
+        t0 = time.perf_counter()
+        cgridder.ms2dirty(uvw, r["freq"], ms_, None, r["npix"], r["npix"], r["cell"], r["cell"],
+                          eps, True)
+        img = numpy.zeros((r["npix"], r["npix"]))
+        img[r["npix"] // 2 + 3, r["npix"] // 2] = 1.0
+        cgridder.dirty2ms(uvw, r["freq"], img, None, r["cell"], r["cell"], eps, True)
+        cpu_t += time.perf_counter() - t0
+        cpu_v += r["nvis"]
+    workload = {"workload": "%d snapshots (32-512 antennas in 1 km, 1-8 chan in 100-200 MHz, "
+                            "1-16 times, 256-2048 px, cell 1/(2.2 max|uv|)), eps 1e-5, FP32 "
+                            "form, Stokes I, invert + predict" % len(raw),
+                "nvis": int(nvis), "snapshots": len(raw),
+                "image_sides": sorted(set(r["npix"] for r in raw))}
+    return _aux_line(args, "Mvis/s invert+predict over 256 uneven snapshots on 1 GB300",
+                     2 * nvis / (ms_batch * 1e-3) / 1e6, "Mvis/s", ms_batch, workload, roof,
+                     kernels, clocks, int(launches / args.steps), dtype="f32",
+                     one_plan_per_snapshot={"ms": round(ms_seq, 1),
+                                            "value": round(2 * nvis / (ms_seq * 1e-3) / 1e6, 2)},
+                     cpu_baseline={"value": round(2 * cpu_v / cpu_t / 1e6, 4), "unit": "Mvis/s",
+                                   "cores": cgridder.max_threads(), "kind": "port",
+                                   "sample": "oracle C gridder (FP64) invert + predict of %d "
+                                             "snapshots (%d vis): %.1f s" % (len(idx), cpu_v,
+                                                                           cpu_t)},
+                     e2e=None)
+
+
+AUX_PATHS = {"weights": bench_weights, "rotation": bench_rotation, "lists": bench_lists,
+             "autograd": bench_autograd, "dft": bench_dft, "batch": bench_batch}
 
 
 def load_peaks():
@@ -888,32 +1397,44 @@ def max_over_ranks(x, world):
 
 
 def run_reference(args):
-    """CPU stand-in for the reference path (ducc0 is not installable here)."""
+    """The reference path's CPU stand-in, timed on the host cores: the oracle's
+    C gridder (ducc0, the reference's gridder, cannot be installed here).
+    Host only: the workload is built with numpy and the GPU library is never
+    loaded.  Each step is one bounded sample (a few w-planes of one
+    polarisation); the line's value extrapolates the measured sample time to
+    the whole step, and says so."""
     rank, world = dist_setup(args)
     if rank != 0:
         return None
-    import torch
-    device = torch.device("cuda", 0) if torch.cuda.is_available() else None
-    if device is None:
-        print(json.dumps({"impl": "reference", "unavailable": "workload generation needs a GPU"}))
-        return None
-    wl = Workload(args.config, args.scale, device)
-    times = []
-    res = None
+    cw = CpuWorkload(args.config, args.scale)
+    samples = []
     for i in range(args.warmup + args.steps):
-        res = cpu_sample(wl, args.cpu_planes)
+        r = cpu_sample(cw, args.cpu_planes)
         if i >= args.warmup:
-            times.append(2 * wl.nvis / (res[0] * 1e6))
-    mvis, cores, desc, _ = res
-    t = float(numpy.mean(times))
-    value = 2 * wl.nvis / t / 1e6
+            samples.append(r)
+    t_sample = float(numpy.mean([r["sample_s"] for r in samples]))
+    t_full = float(numpy.mean([r["full_s"] for r in samples]))
+    value = 2 * cw.nvis / t_full / 1e6
+    r = samples[-1]
+    rc = reduced_case(args.config)
+    acc = cpu_accuracy(rc, r["sigma"], r["cores"])
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mvis/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(t * 1e3, 1), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": workload_config(wl),
-            "cpu_baseline": {"value": round(value, 4), "unit": "Mvis/s", "cores": cores,
-                             "kind": "port", "sample": desc},
+            "ms_per_step": round(t_sample * 1e3, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(cw),
+            "extrapolated": {"value_is_extrapolated": True,
+                             "sample_s_measured": round(t_sample, 3),
+                             "scale_to_full_step": round(r["scale"], 3),
+                             "full_step_s_estimated": round(t_full, 1),
+                             "how": "each step times one sample (%d of %d w-planes, one "
+                                    "polarisation); value = 2 nvis / (sample s x %d/%d planes "
+                                    "x %d pols); ms_per_step is the measured sample"
+                                    % (r["planes"], r["nplanes"], r["nplanes"], r["planes"],
+                                       cw.npol)},
+            "accuracy_reduced_case": {"case": rc["desc"], "epsilon": rc["eps"], "cpu": acc},
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mvis/s", "cores": r["cores"],
+                             "kind": "port", "sample": r["desc"]},
             "e2e": {"value": round(value, 4), "unit": "Mvis/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "note": "ducc0 0.24.0 (the reference's gridder) is not installed on this image; "
@@ -933,6 +1454,43 @@ def workload_config(wl):
             "nvis": wl.nvis, "nrows": wl.nrows, "nchan": wl.nchan, "npol": wl.npv,
             "npixel": wl.npixel, "epsilon": wl.epsilon,
             "l2": "inputs larger than L2 (vis %.1f GB per step)" % (wl.nvis * 8 / 1e9)}
+
+
+# What bounds each kernel of the step (ncu summaries under profiles/).
+KERNEL_BOUND = {
+    "k_grid": "instruction issue around the shared atomics (update rate in roofline.secondary)",
+    "k_degrid": "shared-memory loads and latency (update rate in roofline.secondary)",
+    "k_rows_forward": "instruction issue (DRAM traffic = algorithmic bytes)",
+    "k_rows_inverse": "instruction issue (DRAM traffic = algorithmic bytes)",
+    "k_col_a_inv": "hbm", "k_col_b_inv": "hbm", "k_col_b_pred": "hbm",
+    "k_col_a_pred": "hbm + FP32 sincos", "grid_zero": "hbm (write only)",
+}
+
+
+def mid_like_run(args, device):
+    """The MID-like configuration (197 dishes to 80 km, dec -60, 64 channels
+    over 0.95-1.67 GHz, 4 pols, 512 times, 16384^2 image): 1 warm-up + a
+    few timed FP32 steps, with the FP32 accuracy against the FP64 DFT."""
+    import torch
+    GRID = GRID_BUDGET[0]
+    GRID_BUDGET[0] = int(40 * (1 << 30))  # one 32768^2 x 4-pol plane per batch
+    try:
+        wl = Workload("mid-like", "full", device)
+        ms, out, _, _ = time_steps(wl, "fp32", wl.vis32, wl.wgt32, wl.model32, args.mid_steps,
+                                   args.mid_warmup)
+        dirty, pred, info = out
+        acc = accuracy(wl, dirty, pred, "fp32")
+        del dirty, pred, out
+        res = {"value": round(2 * wl.nvis / (ms * 1e-3) / 1e6, 3), "unit": "Mvis/s",
+               "ms_per_step": round(ms, 1), "steps": args.mid_steps, "warmup": args.mid_warmup,
+               "config": workload_config(wl), "accuracy_fp32": acc,
+               "plan": {k: info[k] for k in ("support", "sigma", "ngrid_x", "nplanes",
+                                             "planes_per_batch", "fft_mode", "own_rows")}}
+        del wl
+    finally:
+        GRID_BUDGET[0] = GRID
+        torch.cuda.empty_cache()
+    return res
 
 
 def main():
@@ -958,7 +1516,8 @@ def main():
     device = torch.device("cuda", torch.cuda.current_device())
     from rascil_gb300 import _lib
     _lib.load()
-    wl = Workload(args.config, args.scale, device)
+    cw = CpuWorkload(args.config, args.scale)
+    wl = Workload(args.config, args.scale, device, cpu=cw)
     sampler = ClockSampler(device.index) if rank == 0 else None
     tuned = tune(wl, "fp32", wl.vis32, wl.wgt32, wl.model32) if args.tune and not args.no_tune \
         else None
@@ -971,7 +1530,11 @@ def main():
     value = world * 2 * wl.nvis / (ms * 1e-3) / 1e6
     acc32 = accuracy(wl, dirty, pred, "fp32")
     del dirty, pred, out
-    roof, kernels = roofline(stats, load_peaks())
+    smem = _lib.smem_peaks(_ptr_stream(torch.cuda.current_stream(device)))
+    roof, kernels = roofline(stats, load_peaks(), smem)
+    for k, b in KERNEL_BOUND.items():
+        if k in kernels:
+            kernels[k]["bound"] = b
     launches = sum(v["launches"] for k, v in stats.items() if not k.startswith("cufft"))
     line = {"metric": METRIC, "value": round(value, 3), "unit": "Mvis/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 2),
@@ -984,6 +1547,7 @@ def main():
                                           "planes_per_batch", "tile", "slab", "beta", "dw",
                                           "fft_mode")},
             "tuning": tuned,
+            "smem_peaks": {"atomics_per_s": smem[0], "loads8_per_s": smem[1]},
             "kernels": kernels}
     torch.cuda.empty_cache()
     if not args.no_fp64:
@@ -1002,14 +1566,33 @@ def main():
     if not args.no_e2e and rank == 0:
         line["e2e"] = e2e_run(wl, args.e2e_steps)
         torch.cuda.empty_cache()
+    cpu_sigma = None
     if not args.no_cpu and rank == 0:
+        # host only: a failure of the CPU gridder is reported in the line and
+        # does not abort the GPU measurement (no device work in this block)
         try:
-            mvis, cores, desc, dt = cpu_sample(wl, args.cpu_planes)
-            line["cpu_baseline"] = {"value": round(mvis, 4), "unit": "Mvis/s", "cores": cores,
-                                    "kind": "port", "sample": desc}
-        except Exception as e:  # reported in the line, not fatal to the GPU measurement
+            r = cpu_sample(cw, args.cpu_planes)
+            line["cpu_baseline"] = {"value": round(r["mvis"], 4), "unit": "Mvis/s",
+                                    "cores": r["cores"], "kind": "port", "sample": r["desc"]}
+            cpu_sigma = r["sigma"]
+        except (OSError, ValueError, IndexError, MemoryError) as e:
             line["cpu_baseline"] = {"value": None, "unit": "Mvis/s", "cores": None,
                                     "kind": "port", "sample": "failed: %s" % e}
+    del wl
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_reduced:
+        # every form's error on one reduced case at the same epsilon, the CPU
+        # path (the reference's stand-in) beside the GPU forms
+        rc = reduced_case(args.config)
+        red = {"case": rc["desc"], "epsilon": rc["eps"],
+               "gpu_fp32": gpu_accuracy(rc, "fp32", device),
+               "gpu_fp64": gpu_accuracy(rc, "fp64", device)}
+        if not args.no_cpu:
+            from oracle import cgridder
+            red["cpu"] = cpu_accuracy(rc, cpu_sigma or 2.0, cgridder.max_threads())
+        line["accuracy_reduced_case"] = red
+    if rank == 0 and not args.no_mid:
+        line["mid_like"] = mid_like_run(args, device)
     if rank == 0:
         print(json.dumps(line))
         if args.json_out:

@@ -254,6 +254,18 @@ int gb_profile_reset(void);
 int gb_profile_count(void);
 int gb_profile_get(int32_t index, char *name, int32_t name_len, double *total_ms,
                    int64_t *launches, double *bytes);
+/* Kernel-weighted updates of the gridding / degridding kernels recorded
+ * under profiling index `index`: one per (item, polarisation, grid cell of
+ * its W x W support, w-plane its support reaches).  0 for other kernels,
+ * and while per-plane statistics are unavailable.  No counterpart in the
+ * reference. */
+int gb_profile_updates(int32_t index, double *updates);
+
+/* Measured shared-memory peaks of the current GPU, for the gridder's and
+ * degridder's update-rate rooflines: conflict-free 32-bit integer atomic
+ * adds per second and conflict-free 8-byte loads per second over all SMs.
+ * Synchronises `stream`.  No counterpart in the reference. */
+int gb_probe_smem_peaks(double *atomics_per_s, double *loads8_per_s, void *stream);
 
 /* Allocation-free w range.  For callers that cannot allocate device memory
  * where they need it -- a host framework that owns every device buffer, or
@@ -264,13 +276,20 @@ int gb_profile_get(int32_t index, char *name, int32_t name_len, double *total_ms
  * reference.
  *   uvw_dev [nrows][3] metres, freq_dev [nchan] Hz (float64, device)
  *   out_dev [4] float64 (device): w_lo, w_hi in wavelengths over all (row,
- *           channel) items -- bit-identical to gb_plan_info's w_lo, w_hi --
- *           then the number of rows with a non-finite coordinate and the
- *           number of non-positive or non-finite frequencies.
- * At most 67,108,864 rows per call (GB_ERR_INVALID_ARG beyond).  The first
- * call on each device looks up the array's device address, so make that
- * first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race. */
+ *           channel) items with a finite uvw row and a positive, finite
+ *           frequency, then the number of rows with a non-finite coordinate
+ *           and the number of non-positive or non-finite frequencies.  For
+ *           input the planner accepts (both counts zero) and a w-stacking
+ *           plan, w_lo and w_hi are bit-identical to gb_plan_info's; plans
+ *           without w-stacking report 0, 0 there.  When every row or every
+ *           frequency is invalid, w_lo = +inf and w_hi = -inf.
+ * At most 67,108,864 rows per call (GB_ERR_INVALID_ARG beyond).  A call
+ * outside a stream capture looks up the array's device address on the
+ * current device (a context recreated after cudaDeviceReset gets a new
+ * one); a call inside a capture reuses the address from the last call on
+ * that device outside a capture, so make one call before any capture.  All
+ * calls share the array: calls that overlap on the GPU (other streams,
+ * other host threads) race, and the caller must serialise them. */
 int gb_wrange_noalloc(const double *uvw_dev, const double *freq_dev, int64_t nrows,
                       int32_t nchan, double *out_dev, void *stream);
 

@@ -5,7 +5,8 @@ The reference ships that kernel as a source string, ``cuda_kernel_source``
 in ``rascil/processing_components/imaging/dft.py:181-258``, compiled at run
 time through CuPy (``dft.py:284-332``).  CuPy is not installed, so:
 
-* ``extract(ref_root)`` (runs where the reference tree is present) copies
+* ``extract(ref_root)`` (runs where the reference tree is present; its root
+  is an argument, or RASCIL_REFERENCE_ROOT for the command line) copies
   the string into ``oracle/_ref/dft_kernel_ref.cu`` -- an untracked build
   output, never committed;
 * ``build()`` (runs anywhere nvcc is) compiles that file together with
@@ -27,7 +28,11 @@ KERNEL = os.path.join(REF_DIR, "dft_kernel_ref.cu")
 LIB = os.path.join(REF_DIR, "libref_dft.so")
 
 
-def extract(ref_root="/root/reference"):
+def extract(ref_root):
+    """Copy the kernel string out of the reference tree rooted at
+    ``ref_root`` (None or a missing tree: nothing to do, returns None)."""
+    if not ref_root:
+        return None
     path = os.path.join(ref_root, "rascil", "processing_components", "imaging", "dft.py")
     if not os.path.exists(path):
         return None
@@ -60,4 +65,7 @@ def build(force=False):
 
 
 if __name__ == "__main__":
-    print(extract(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"), build(force=True))
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RASCIL_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_ref_dft.py REFERENCE_ROOT (or set RASCIL_REFERENCE_ROOT)")
+    print(extract(root), build(force=True))

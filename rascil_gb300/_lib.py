@@ -125,6 +125,8 @@ SIGNATURES = {
     "gb_profile_count": (_c.c_int, []),
     "gb_profile_get": (_c.c_int, [_c.c_int32, _c.c_char_p, _c.c_int32, _dp,
                                   _c.POINTER(_c.c_int64), _dp]),
+    "gb_profile_updates": (_c.c_int, [_c.c_int32, _dp]),
+    "gb_probe_smem_peaks": (_c.c_int, [_dp, _dp, _vp]),
     "gb_apply_gains": (_c.c_int, [_vp, _vp, _vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32,
                                   _c.c_int32, _vp, _vp]),
     "gb_gain_gradient": (_c.c_int, [_vp, _vp, _vp, _vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32,
@@ -198,6 +200,18 @@ def profile_read():
         n = ctypes.c_int64()
         b = ctypes.c_double()
         check(lib.gb_profile_get(i, name, 64, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(b)))
+        u = ctypes.c_double()
+        check(lib.gb_profile_updates(i, ctypes.byref(u)))
         if n.value:
-            out[name.value.decode()] = {"ms": ms.value, "launches": n.value, "bytes": b.value}
+            out[name.value.decode()] = {"ms": ms.value, "launches": n.value, "bytes": b.value,
+                                        "updates": u.value}
     return out
+
+
+def smem_peaks(stream=None):
+    """Measured (conflict-free 32-bit shared atomic adds per second,
+    conflict-free 8-byte shared loads per second) of the current GPU."""
+    a, l = ctypes.c_double(), ctypes.c_double()
+    check(load().gb_probe_smem_peaks(ctypes.byref(a), ctypes.byref(l), stream),
+          "gb_probe_smem_peaks")
+    return a.value, l.value

@@ -516,10 +516,14 @@ static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
       GB_CUDA(cudaMemsetAsync(grid, 0, sizeof(C) * (size_t)nb * NP * plane, s));
     }
     {
-      // items and their vis read once; the grid rows they reach written once
+      // items and their gridded values read once; every grid cell of the
+      // (plane, tile) pairs they reach read and written once (the float2
+      // atomic flush is a read-modify-write), else the rows they reach
+      const double cells = p->touched_cells(b0, nb);
+      const double gmove = cells > 0.0 ? 2.0 * cells * NP * sizeof(C) : used * gbytes;
       ProfScope ps(kProfGrid, s,
-                   (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) +
-                       used * gbytes);
+                   (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) + gmove,
+                   p->item_planes(b0, nb) * g.W * g.W * NP);
       if (group_lanes(g.W) == 8)
         k_grid<R, NP, 8><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks,
                                                                 chunk_off, b0, nb, grid,

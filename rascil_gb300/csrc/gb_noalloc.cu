@@ -119,9 +119,14 @@ __global__ void k_wrange_finish(const double *__restrict__ parts, int nparts,
   }
 }
 
-// Device address of the scratch array for the current device, looked up
-// once per device (with that device current) and cached.
-static int scratch_address(double **ptr) {
+// Device address of the scratch array for the current device.  Outside a
+// stream capture the address is looked up on every call (with that device
+// current; the lookup allocates nothing), so a context torn down and
+// recreated -- cudaDeviceReset reloads the module at a new address -- is
+// picked up.  Inside a capture, where the lookup is not allowed, the
+// address cached by the last call outside a capture on this device is
+// used; there must have been one.
+static int scratch_address(cudaStream_t s, double **ptr) {
   static std::mutex mu;
   static double *cached[kNoAllocMaxDevices] = {};
   int dev = 0;
@@ -130,11 +135,17 @@ static int scratch_address(double **ptr) {
     set_error("gb_wrange_noalloc: device ordinal %d beyond %d", dev, kNoAllocMaxDevices);
     return GB_ERR_INVALID_ARG;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  GB_CUDA(cudaStreamIsCapturing(s, &cap));
   std::lock_guard<std::mutex> lk(mu);
-  if (!cached[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void *p = nullptr;
     GB_CUDA(cudaGetSymbolAddress(&p, g_wrange_scratch));
     cached[dev] = static_cast<double *>(p);
+  } else if (!cached[dev]) {
+    set_error("gb_wrange_noalloc: the first call on device %d is inside a stream capture; "
+              "make one call outside a capture first", dev);
+    return GB_ERR_INVALID_ARG;
   }
   *ptr = cached[dev];
   return GB_OK;
@@ -164,10 +175,10 @@ int gb_wrange_noalloc(const double *uvw_dev, const double *freq_dev, int64_t nro
               (long long)nrows, (long long)max_rows);
     return GB_ERR_INVALID_ARG;
   }
-  double *parts = nullptr;
-  int rc = scratch_address(&parts);
-  if (rc) return rc;
   cudaStream_t s = (cudaStream_t)stream;
+  double *parts = nullptr;
+  int rc = scratch_address(s, &parts);
+  if (rc) return rc;
   const int nparts = (int)((nrows + kNoAllocRowsPerPart - 1) / kNoAllocRowsPerPart);
   k_wrange_parts<<<nparts, kThreads, 0, s>>>(uvw_dev, nrows, parts);
   GB_LAUNCH_CHECK("k_wrange_parts");

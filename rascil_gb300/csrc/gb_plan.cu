@@ -507,6 +507,100 @@ __global__ void k_row_mask(const Geom g, const Chunk *__restrict__ chunks,
   }
 }
 
+// Profiling statistics (one thread per chunk): mark every (w-plane, uv
+// tile) pair the chunk's items reach and count items per first w-plane.
+template <typename Item>
+__global__ void k_plane_stats(const Geom g, const Item *__restrict__ items,
+                              const Chunk *__restrict__ chunks,
+                              const uint32_t *__restrict__ chunk_off, uint8_t *__restrict__ tmask,
+                              unsigned long long *__restrict__ k0_count) {
+  const uint32_t nch = chunk_off[g.nbuckets];
+  const int ntiles = g.ntu * g.ntv;
+  const int wd = g.do_w ? g.W : 1;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nch; c += gridDim.x * blockDim.x) {
+    const Chunk ch = chunks[c];
+    const int slab = (int)(ch.bucket / (uint32_t)ntiles);
+    const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
+    int lo = 1 << 30, hi = -1;
+    uint32_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t j = ch.begin; j < ch.end; ++j) {
+      const int lk = (int)((items[j].loc >> 16) & 0xffu);
+      lo = min(lo, lk);
+      hi = max(hi, lk);
+      if (lk < 8)
+        ++cnt[lk];
+      else
+        atomicAdd(&k0_count[slab * g.S + lk], 1ull);
+    }
+    for (int lk = 0; lk < 8; ++lk)
+      if (cnt[lk]) atomicAdd(&k0_count[slab * g.S + lk], (unsigned long long)cnt[lk]);
+    for (int k = slab * g.S + lo; hi >= 0 && k < min(slab * g.S + hi + wd, g.nplanes); ++k)
+      tmask[(int64_t)k * ntiles + tile] = 1;
+  }
+}
+
+// Cells per w-plane in the marked tiles: T x T per tile (clipped at the
+// grid's edge) plus the W - 1 halo strips and corner that spill into an
+// unmarked neighbour (support footprints start inside their tile).
+__global__ void k_plane_cells(const Geom g, const uint8_t *__restrict__ tmask,
+                              unsigned long long *__restrict__ cells) {
+  const int ntiles = g.ntu * g.ntv;
+  for (int k = blockIdx.y; k < g.nplanes; k += gridDim.y) {
+    const uint8_t *m = tmask + (int64_t)k * ntiles;
+    unsigned long long acc = 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles;
+         t += gridDim.x * blockDim.x) {
+      if (!m[t]) continue;
+      const int tv = t / g.ntu, tu = t - tv * g.ntu;
+      const int wu = min(g.T, g.ngx - tu * g.T), wv = min(g.T, g.ngy - tv * g.T);
+      const int tu1 = tu + 1 == g.ntu ? 0 : tu + 1, tv1 = tv + 1 == g.ntv ? 0 : tv + 1;
+      const int h = g.W - 1;
+      acc += (unsigned long long)wu * wv;
+      if (!m[tv * g.ntu + tu1]) acc += (unsigned long long)h * wv;
+      if (!m[tv1 * g.ntu + tu]) acc += (unsigned long long)wu * h;
+      if (!m[tv1 * g.ntu + tu1]) acc += (unsigned long long)h * h;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&cells[k], acc);
+  }
+}
+
+// Host copies of the per-plane statistics (profiling only; synchronises).
+template <typename Item>
+static int plane_stats(gb_plan *p, cudaStream_t s) {
+  const Geom &g = p->g;
+  const int64_t ntiles = (int64_t)g.ntu * g.ntv;
+  const size_t mbytes = (size_t)g.nplanes * (size_t)ntiles;
+  p->plane_cells.clear();
+  p->plane_k0.clear();
+  if (mbytes > ((size_t)1 << 30)) return GB_OK;  // too large to be worth it: no statistics
+  uint8_t *tmask = nullptr;
+  unsigned long long *cnt = nullptr;
+  GB_CUDA(cudaMallocAsync((void **)&tmask, mbytes, s));
+  GB_CUDA(cudaMallocAsync((void **)&cnt, 16 * (size_t)g.nplanes, s));
+  GB_CUDA(cudaMemsetAsync(tmask, 0, mbytes, s));
+  GB_CUDA(cudaMemsetAsync(cnt, 0, 16 * (size_t)g.nplanes, s));
+  const unsigned cb = (unsigned)std::min<int64_t>(
+      ((int64_t)p->max_chunks + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
+  k_plane_stats<Item><<<cb, kThreads, 0, s>>>(g, p->at<Item>(p->off_items),
+                                              p->at<Chunk>(p->off_chunks),
+                                              p->at<uint32_t>(p->off_chunk_off), tmask,
+                                              cnt + g.nplanes);
+  GB_LAUNCH_CHECK("k_plane_stats");
+  const dim3 grid((unsigned)std::min<int64_t>((ntiles + kThreads - 1) / kThreads, 64),
+                  (unsigned)std::min(g.nplanes, 65535));
+  k_plane_cells<<<grid, kThreads, 0, s>>>(g, tmask, cnt);
+  GB_LAUNCH_CHECK("k_plane_cells");
+  std::vector<unsigned long long> h(2 * (size_t)g.nplanes);
+  GB_CUDA(cudaMemcpyAsync(h.data(), cnt, 16 * (size_t)g.nplanes, cudaMemcpyDeviceToHost, s));
+  cudaFreeAsync(tmask, s);
+  cudaFreeAsync(cnt, s);
+  GB_CUDA(cudaStreamSynchronize(s));
+  p->plane_cells.assign(h.begin(), h.begin() + g.nplanes);
+  p->plane_k0.assign(h.begin() + g.nplanes, h.end());
+  return GB_OK;
+}
+
 // exp(+2 pi i m / n), m < n, rounded from FP64.
 __global__ void k_twiddles(int n, float2 *__restrict__ tw) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -815,6 +909,10 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
                               cudaMemcpyDeviceToHost, s));
       GB_CUDA(cudaStreamSynchronize(s));
     }
+  }
+  if (prof_on()) {
+    const int rc2 = plane_stats<Item>(p, s);
+    if (rc2) return rc2;
   }
   return GB_OK;
 }

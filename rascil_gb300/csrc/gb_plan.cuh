@@ -56,6 +56,29 @@ struct gb_plan {
   int grid_blocks = 0, degrid_blocks = 0;  // persistent grid sizes
   std::vector<uint32_t> slab_items;        // host copy: first item of each slab (+ total)
   std::vector<uint8_t> mask_host;          // host copy of the occupancy mask (profiling)
+  // profiling only: per w-plane, grid cells in the (plane, uv tile) pairs
+  // some item reaches (tile cells plus the support halo spilling into
+  // tiles nothing reaches), and items whose first plane is that plane
+  std::vector<int64_t> plane_cells, plane_k0;
+
+  // Grid cells the items of planes [b0, b0 + nb) reach (0 when unknown).
+  double touched_cells(int b0, int nb) const {
+    if (plane_cells.empty()) return 0.0;
+    double c = 0.0;
+    for (int k = b0; k < b0 + nb && k < (int)plane_cells.size(); ++k) c += (double)plane_cells[k];
+    return c;
+  }
+
+  // (item, plane) pairs with the item's support reaching the plane, over
+  // planes [b0, b0 + nb): each is W^2 cell updates per polarisation.
+  double item_planes(int b0, int nb) const {
+    if (plane_k0.empty()) return 0.0;
+    const int wd = g.do_w ? g.W : 1;
+    double n = 0.0;
+    for (int k = b0; k < b0 + nb && k < (int)plane_k0.size(); ++k)
+      for (int k0 = std::max(0, k - wd + 1); k0 <= k; ++k0) n += (double)plane_k0[k0];
+    return n;
+  }
 
   // Fraction of the rows of planes [b0, b0 + nb) that visibilities reach
   // (occupancy mask; 1 without one).  Profiling byte counts only.

@@ -634,10 +634,13 @@ static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *
     if (rc) return rc;
     {
       const double nbi = (double)p->batch_items(b0, nb);
-      // items read, their vis written once; the grid rows they reach read once
+      // items read, their vis written once; the grid cells they reach read
+      // once (the cells of the (plane, tile) pairs reached, else the rows)
+      const double cells = p->touched_cells(b0, nb);
+      const double gread = cells > 0.0 ? cells * NP * sizeof(C) : p->used_rows(b0, nb) * gbytes;
       ProfScope ps(kProfDegrid, s,
-                   nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) +
-                       p->used_rows(b0, nb) * gbytes);
+                   nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) + gread,
+                   p->item_planes(b0, nb) * g.W * g.W * NP);
       if constexpr (std::is_same<R, float>::value) {
         launch_degrid_lane<NP>(p, (unsigned)p->degrid_blocks, degrid_lane_smem_bytes(p), s, items,
                                chunks, chunk_off, b0, nb, grid, vis_c, npv,

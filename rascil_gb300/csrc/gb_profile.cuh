@@ -45,16 +45,18 @@ extern const char *kProfNames[kProfCount];
 bool prof_on();
 
 // Records an event pair around its lifetime on stream `s` when profiling
-// is on; `bytes` is the algorithmic traffic of the enclosed launch.
+// is on; `bytes` is the algorithmic traffic of the enclosed launch and
+// `updates` (gridding / degridding kernels only) the number of
+// (item, polarisation, grid cell) kernel-weighted updates it performs.
 class ProfScope {
  public:
-  ProfScope(int id, cudaStream_t s, double bytes);
+  ProfScope(int id, cudaStream_t s, double bytes, double updates = 0.0);
   ~ProfScope();
 
  private:
   int id_;
   cudaStream_t s_;
-  double bytes_;
+  double bytes_, updates_;
   bool active_ = false;
   cudaEvent_t a_ = nullptr;
 };

@@ -1,9 +1,9 @@
 """Generate golden vectors by running the reference's own code.
 
 Run in a checkout where the reference tree is available (its path is the
-first argument, default /root/reference):
+first argument, or RASCIL_REFERENCE_ROOT):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py REFERENCE_ROOT
 
 RASCIL itself cannot be imported here (astropy, xarray, ducc0 are absent),
 so the functions on this path that are plain numpy are loaded directly:
@@ -370,4 +370,7 @@ def rotation_golden(rascil, cs, rng):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("RASCIL_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set RASCIL_REFERENCE_ROOT)")
+    main(root)

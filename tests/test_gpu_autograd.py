@@ -162,3 +162,40 @@ def test_gradient_descent_reduces_the_loss():
     assert losses[-1] < 0.1 * losses[0]
     assert int(torch.argmax(x.detach()).item()) == 30 * 64 + 37
     plan.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("fp32", 1e-4), ("fp64", 1e-9)])
+def test_predict_adjoint_dot_product_full_size(precision, tol):
+    """The differentiable-predict configuration at its stated size: a 2048^2
+    sky, 128 antennas (8,128 baselines) in a 1 km disk, 8 channels over
+    150-158 MHz, 64 times (4,161,536 visibilities): Re<y, A x> = <x, A^H y>
+    through the autograd Function (A^H = the gridder applied in backward)."""
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.autograd import predict
+    from rascil_gb300.wgridder import Plan
+    uvw, freq, pc, cfg = sim.observation("gain-solve", seed=0)
+    assert uvw.shape[:2] == (64, 8128) and len(freq) == 8 and cfg["npixel"] == 2048
+    fu = torch.from_numpy(uvw.reshape(-1, 3) * numpy.array([-1.0, 1.0, -1.0])).cuda()
+    f = torch.from_numpy(freq.copy()).cuda()
+    eps = 1e-5 if precision == "fp32" else 1e-12
+    plan = Plan(fu, f, 2048, 2048, cfg["cellsize"], cfg["cellsize"], eps, True, npol=1,
+                precision=precision)
+    try:
+        g = torch.Generator(device="cuda")
+        g.manual_seed(3)
+        x = torch.randn((1, 2048, 2048), generator=g, device="cuda",
+                        dtype=plan.real_dtype).requires_grad_(True)
+        y = torch.randn((plan.nrows, plan.nchan, 1, 2), generator=g, device="cuda",
+                        dtype=plan.real_dtype)
+        y = torch.view_as_complex(y).contiguous()
+        v = predict(x, plan)
+        lhs = torch.real(torch.vdot(y.reshape(-1).to(torch.complex128),
+                                    v.reshape(-1).to(torch.complex128)))
+        lhs.backward()
+        rhs = (x.detach().double() * x.grad.double()).sum()
+        # Cauchy-Schwarz scale of the inner product
+        scale = float(torch.linalg.vector_norm(v.detach().to(torch.complex128)) *
+                      torch.linalg.vector_norm(y.to(torch.complex128)))
+        assert abs(float(lhs) - float(rhs)) <= tol * scale, (float(lhs), float(rhs), scale)
+    finally:
+        plan.close()

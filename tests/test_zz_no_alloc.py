@@ -30,8 +30,15 @@ def test_wrange_noalloc_matches_planner_twice():
     from rascil_gb300 import _lib, wgridder
     lib = _lib.load()
     out = torch.full((4,), float("nan"), dtype=torch.float64, device="cuda")
-    for seed, nrows, nchan in ((0, 200_003, 3), (1, 9_000, 7)):
+    # the wider w range over many rows first (49 partials), then fewer rows
+    # (3 partials) whose w range lies strictly inside it: a reduction that
+    # read the first call's leftover partials would widen the second range
+    raw = []
+    for seed, nrows, nchan in ((1, 200_003, 7), (0, 9_000, 3)):
         uvw, freq = _problem(seed, nrows, nchan)
+        raw.append((float(uvw[:, 2].min()), float(uvw[:, 2].max())))
+        if len(raw) == 2:  # the case is meaningful only if the second range is inside
+            assert raw[0][0] < raw[1][0] and raw[1][1] < raw[0][1]
         plan = wgridder.Plan(uvw, freq, 64, 64, 2e-3, 2e-3, 1e-5, True, precision="fp32")
         ref = plan.info
         plan.close()
