@@ -76,6 +76,8 @@ def parse():
                     help="untimed FP64-form steps (the FP32 warm-up already built the caches)")
     ap.add_argument("--tune", action="store_true",
                     help="run the per-shape autotuner first (untimed) and use its choice")
+    ap.add_argument("--tune-seconds", type=float, default=120.0,
+                    help="time budget of the autotuner's search")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the per-shape autotuner (use cached or default plan parameters)")
     ap.add_argument("--plan", default=None,
@@ -260,23 +262,35 @@ FFT_MODE = ["auto"]
 FIXED_PLAN = [None]
 
 
-def make_plan(wl, precision, params=None):
+def make_plan(wl, precision, params=None, bind=True):
     from rascil_gb300.wgridder import Plan
     params = params or FIXED_PLAN[0] or {}
     return Plan(wl.uvw, wl.freq_dev, wl.npixel, wl.npixel, wl.cell, wl.cell, wl.epsilon, True,
                 npol=wl.npol, precision=precision, grid_budget_bytes=GRID_BUDGET[0],
                 sigma=params.get("sigma", 0.0), tile=params.get("tile", 0),
-                slab=params.get("slab", 0), fft_mode=FFT_MODE[0])
+                slab=params.get("slab", 0), planes_per_batch=params.get("planes", 0),
+                fft_mode=FFT_MODE[0], bind=bind)
 
 
-def tune(wl, precision, vis, wgt, model):
-    """Per-shape autotuning (untimed): the plan parameters the timed steps
-    then pick up from the tuning cache."""
+def tune(wl, precision, vis, wgt, model, max_seconds=120.0):
+    """Per-shape autotuning (untimed): a coordinate search from the
+    planner's own choice over sigma, tile, slab and planes per batch; the
+    timed steps then pick the winner up from the tuning cache."""
     from rascil_gb300 import tuning
     key = tuning.shape_key(wl.npixel, wl.npixel, wl.cell, wl.npol, precision, wl.epsilon, True,
                            wl.nrows, wl.nchan)
-    best, timings = tuning.autotune(key, lambda prm: step(wl, precision, vis, wgt, model, prm))
-    return {"key": key, "chosen": best, "candidate_ms": timings}
+    tuning.forget(key)
+    p0 = make_plan(wl, precision, bind=False)
+    info = p0.info
+    p0.close()
+    start = {"sigma": info["sigma"], "tile": info["tile"], "slab": info["slab"],
+             "planes": info["planes_per_batch"]}
+    plane_bytes = info["ngrid_x"] * info["ngrid_y"] * wl.npol * (8 if precision == "fp32"
+                                                                  else 16)
+    best, timings = tuning.autotune(key, lambda prm: step(wl, precision, vis, wgt, model, prm),
+                                    start=start, plane_bytes=plane_bytes,
+                                    max_seconds=max_seconds)
+    return {"key": key, "planner_choice": start, "chosen": best, "candidate_ms": timings}
 
 
 def step(wl, precision, vis, wgt, model, params=None):
@@ -1519,8 +1533,8 @@ def main():
     cw = CpuWorkload(args.config, args.scale)
     wl = Workload(args.config, args.scale, device, cpu=cw)
     sampler = ClockSampler(device.index) if rank == 0 else None
-    tuned = tune(wl, "fp32", wl.vis32, wl.wgt32, wl.model32) if args.tune and not args.no_tune \
-        else None
+    tuned = tune(wl, "fp32", wl.vis32, wl.wgt32, wl.model32, args.tune_seconds) \
+        if args.tune and not args.no_tune else None
     if world > 1:
         torch.distributed.barrier()
     ms, out, clocks, stats = time_steps(wl, "fp32", wl.vis32, wl.wgt32, wl.model32, args.steps,

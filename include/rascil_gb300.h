@@ -83,7 +83,9 @@ typedef struct {
   double epsilon;      /* requested accuracy (ducc0 epsilon)                   */
   int32_t do_wstacking;/* ducc0 do_wstacking                                   */
   int32_t precision;   /* gb_precision                                         */
-  double sigma;        /* grid oversampling; 0 = default (2.0)                 */
+  double sigma;        /* grid oversampling (1.25, 1.5, 1.75, 2); 0 = the one of
+                          least modelled cost (gridding work against per-plane
+                          transform work), 2 unless another is 10 % cheaper */
   int32_t support;     /* kernel support W; 0 = smallest W meeting epsilon     */
   int32_t tile;        /* uv tile side in cells; 0 = default                   */
   int32_t slab;        /* w-planes per bucket slab; 0 = default                */
@@ -100,6 +102,8 @@ typedef struct {
    * and ng.py's uvw (u and w negated), s = (-l, m, -(n - 1)).  All zero:
    * no rotation.                                                          */
   double phase_shift[3];
+  int32_t planes_per_batch; /* w-planes transformed per batch; 0 = as many as
+                               grid_budget_bytes holds (at least one)        */
 } gb_plan_params;
 
 /* Geometry the planner chose; all host values. */

@@ -58,6 +58,7 @@ class PlanParams(_c.Structure):
         ("grid_budget_bytes", _c.c_int64),
         ("fft_mode", _c.c_int32),
         ("phase_shift", _c.c_double * 3),
+        ("planes_per_batch", _c.c_int32),
     ]
 
 

@@ -57,11 +57,67 @@ static int good_size(int n) {
   }
 }
 
+static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi, double sigma,
+                               Geom &g);
+
+// Cost model of one direction (invert or predict) of a plan, in seconds on
+// GB300, for choosing the grid oversampling when the caller leaves it at 0
+// (ducc0 makes the same choice internally from a cost model): gridding work
+// per (item, w-plane its support reaches, polarisation), growing as W^2,
+// plus per-plane transform work per grid cell and polarisation -- the
+// library's pruned row/column transforms where they apply, batched 2-D
+// cuFFT plans with separate zeroing and screen passes otherwise.  Constants
+// measured on the LOW-like workload (k_grid / k_degrid_lane per update; the
+// column-mode passes and cuFFT planes per cell).
+constexpr double kCostItemPlane[2] = {9.3e-11, 2.5e-9};  // FP32, FP64 (at W = 7)
+constexpr double kCostCellColumns = 4.7e-12;
+constexpr double kCostCellCufft[2] = {8.7e-12, 1.8e-11};
+
+static bool columns_apply(const gb_plan_params *p, const Geom &g) {
+  int n1, n2;
+  return p->precision == GB_FP32 && p->fft_mode != GB_FFT_CUFFT_2D && g.ngy == 2 * g.ny &&
+         (g.ngx - g.nx) % 4 == 0 && column_split(g.ngy, n1, n2);
+}
+
+static double plan_cost(const gb_plan_params *p, const Geom &g) {
+  const int f = p->precision == GB_FP64 ? 1 : 0;
+  const double items = (double)p->nrows * (double)p->nchan;
+  const double wp = g.do_w ? g.W : 1;
+  const double grid = items * g.NP * wp * (g.W * g.W / 49.0) * kCostItemPlane[f];
+  const double cell = columns_apply(p, g) ? kCostCellColumns : kCostCellCufft[f];
+  return grid + (double)g.nplanes * g.NP * (double)g.ngx * (double)g.ngy * cell;
+}
+
 int plan_geometry(const gb_plan_params *p, double w_lo, double w_hi, Geom &g) {
   if (!p) {
     set_error("params is NULL");
     return GB_ERR_INVALID_ARG;
   }
+  if (p->sigma > 0.0) return plan_geometry_sigma(p, w_lo, w_hi, p->sigma, g);
+  // sigma 0: the tabulated oversampling of least modelled cost; 2.0 unless
+  // another is at least 10 % cheaper (power-of-two grids for power-of-two
+  // images, the library's own transforms)
+  static const double kSigmas[] = {2.0, 1.75, 1.5, 1.25};
+  double best = 0.0;
+  bool found = false;
+  for (double sg : kSigmas) {
+    Geom t;
+    if (plan_geometry_sigma(p, w_lo, w_hi, sg, t) != GB_OK) continue;
+    if (p->fft_mode == GB_FFT_COLUMNS && !columns_apply(p, t)) continue;
+    const double c = plan_cost(p, t) * (sg == 2.0 ? 0.9 : 1.0);
+    if (!found || c < best) {
+      best = c;
+      g = t;
+      found = true;
+    }
+  }
+  if (!found) return plan_geometry_sigma(p, w_lo, w_hi, 2.0, g);  // for its error message
+  set_error("");
+  return GB_OK;
+}
+
+static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi, double sigma,
+                               Geom &g) {
   if (p->nrows <= 0 || p->nchan <= 0) {
     set_error("nrows and nchan must be positive (got %lld, %d)", (long long)p->nrows,
               p->nchan);
@@ -99,7 +155,6 @@ int plan_geometry(const gb_plan_params *p, double w_lo, double w_hi, Geom &g) {
     return GB_ERR_INVALID_ARG;
   }
   memset(&g, 0, sizeof(g));
-  const double sigma = p->sigma > 0.0 ? p->sigma : 2.0;
   const int ndim = p->do_wstacking ? 3 : 2;
   int W = 0;
   double beta = 0.0;
@@ -210,7 +265,7 @@ int plan_geometry(const gb_plan_params *p, double w_lo, double w_hi, Geom &g) {
       p->grid_budget_bytes > 0 ? p->grid_budget_bytes : (int64_t)32 << 30;
   const int64_t per_plane =
       (int64_t)g.NP * g.ngx * g.ngy * (int64_t)cplx_bytes(p->precision);
-  int64_t B = budget / per_plane;
+  int64_t B = p->planes_per_batch > 0 ? (int64_t)p->planes_per_batch : budget / per_plane;
   if (B < 1) B = 1;
   if (B > g.nplanes) B = g.nplanes;
   g.B = (int)B;

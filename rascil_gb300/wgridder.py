@@ -61,6 +61,10 @@ class Plan:
         FP32 form, power-of-two grid height), "columns" (require them) or
         "cufft2d" (batched 2-D cuFFT plans); ``info["fft_mode"]`` reports
         the one in use (2 = columns, 1 = cufft2d)
+    :param sigma: grid oversampling (1.25, 1.5, 1.75, 2); 0 = the planner's
+        choice by its cost model (or a cached autotuning result)
+    :param planes_per_batch: w-planes per transform batch (0: what
+        ``grid_budget_bytes`` holds)
     :param phase_shift: (s0, s1, s2) of a tangent-plane phase rotation fused
         into the plan's per-item factors: ms2dirty grids vis times
         exp(+2 pi i (u s0 + v s1 + w s2) f/c) (not for a PSF), dirty2ms
@@ -70,7 +74,7 @@ class Plan:
     def __init__(self, uvw, freq, npix_x, npix_y, pixsize_x, pixsize_y, epsilon,
                  do_wstacking, npol=1, precision="fp32", sigma=0.0, support=0, tile=0,
                  slab=0, grid_budget_bytes=0, bind=True, fft_mode="auto",
-                 phase_shift=(0.0, 0.0, 0.0)):
+                 phase_shift=(0.0, 0.0, 0.0), planes_per_batch=0):
         lib = _lib.load()
         _require_cuda(uvw, "uvw")
         _require_cuda(freq, "freq")
@@ -89,9 +93,12 @@ class Plan:
         self.npix_x, self.npix_y = int(npix_x), int(npix_y)
         self.shape_key = tuning.shape_key(npix_x, npix_y, pixsize_x, npol, precision, epsilon,
                                           do_wstacking, self.nrows, self.nchan)
-        if not sigma and not tile and not slab:
+        if not sigma and not tile and not slab and not planes_per_batch:
             chosen = tuning.choose(self.shape_key, npix_x, npix_y, self.nrows, self.nchan)
             sigma, tile, slab = chosen["sigma"], chosen["tile"], chosen["slab"]
+            planes_per_batch = chosen.get("planes", 0)
+            if planes_per_batch:
+                grid_budget_bytes = 0
         self._uvw, self._freq = uvw, freq
         p = _lib.PlanParams()
         p.nrows = self.nrows
@@ -110,6 +117,7 @@ class Plan:
         p.slab = int(slab)
         p.grid_budget_bytes = int(grid_budget_bytes)
         p.fft_mode = _FFT_MODE[fft_mode]
+        p.planes_per_batch = int(planes_per_batch)
         shift = [float(x) for x in phase_shift]
         if len(shift) != 3:
             raise ValueError("phase_shift must hold three coefficients")

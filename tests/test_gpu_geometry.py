@@ -44,14 +44,15 @@ def _geometry(name, ntimes, nchan, npixel, cell, nsrc=40, seed=0):
 
 
 def _check(fu, freq, dirty, src_pix, npix, cell, precision, eps, tol, fft_expect=None,
-           nrows_check=192, npix_check=48):
+           nrows_check=192, npix_check=48, sigma=0.0):
     from rascil_gb300.wgridder import Plan
     rng = numpy.random.default_rng(11)
     cdt = torch.complex128 if precision == "fp64" else torch.complex64
     rdt = torch.float64 if precision == "fp64" else torch.float32
     u = torch.from_numpy(fu.copy()).cuda()
     f = torch.from_numpy(freq.copy()).cuda()
-    plan = Plan(u, f, npix, npix, cell, cell, eps, True, npol=1, precision=precision)
+    plan = Plan(u, f, npix, npix, cell, cell, eps, True, npol=1, precision=precision,
+                sigma=sigma)
     try:
         if fft_expect is not None:
             assert (plan.info["fft_mode"], plan.info["own_rows"]) == fft_expect, plan.info
@@ -111,4 +112,13 @@ def test_wide_grid_column_mode_against_cpu_oracle(npix, own_rows):
     of 8192 and 16384 cells (the headline's transforms), LOW-like baselines."""
     fu, freq, dirty, src = _geometry("low-like", 1, 2, npix, 1e-5)
     _check(fu, freq, dirty, src, npix, 1e-5, "fp32", 1e-5, 1e-5, fft_expect=(2, own_rows),
-           nrows_check=128, npix_check=32)
+           nrows_check=128, npix_check=32, sigma=2.0)
+
+
+@pytest.mark.parametrize("sigma", [1.25, 1.5, 1.75])
+def test_low_like_geometry_other_oversampling(sigma):
+    """The FP32 form at every other tabulated grid oversampling (batched
+    cuFFT transforms, larger supports), LOW-like baselines."""
+    fu, freq, dirty, src = _geometry("low-like", 2, 2, 1024, 1e-5)
+    info = _check(fu, freq, dirty, src, 1024, 1e-5, "fp32", 1e-5, 1e-5, sigma=sigma)
+    assert info["sigma"] == sigma and info["fft_mode"] == 1

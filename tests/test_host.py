@@ -203,7 +203,8 @@ def test_planner_geometry_matches_oracle(precision, eps, do_w, npix, cell):
     from oracle import wgridder as owg
     from rascil_gb300.wgridder import plan_geometry
     w_lo, w_hi = -1234.5, 4321.25
-    info = plan_geometry(npix, npix, cell, cell, eps, do_w, w_lo, w_hi, precision=precision)
+    info = plan_geometry(npix, npix, cell, cell, eps, do_w, w_lo, w_hi, precision=precision,
+                         sigma=2.0)
     op = owg.Plan(npix, npix, cell, cell, eps, do_w, w_lo, w_hi, fp32=precision == "fp32")
     assert info["support"] == op.W and info["beta"] == op.beta
     assert info["ngrid_x"] == op.ngx and info["ngrid_y"] == op.ngy
@@ -278,3 +279,32 @@ def test_empty_visibilities_need_no_device():
     p = predict_ng(b, model)
     assert p is not b and p["vis"].data.shape == b["vis"].data.shape
     assert weight_visibility(b, model) is b
+
+
+@pytest.mark.parametrize("sigma", [1.25, 1.5, 1.75])
+def test_planner_geometry_matches_oracle_other_sigmas(sigma):
+    from oracle import wgridder as owg
+    from rascil_gb300.wgridder import plan_geometry
+    info = plan_geometry(1024, 1024, 1e-4, 1e-4, 1e-5, True, -800.0, 2500.0, precision="fp32",
+                         sigma=sigma)
+    op = owg.Plan(1024, 1024, 1e-4, 1e-4, 1e-5, True, -800.0, 2500.0, sigma=sigma, fp32=True)
+    assert (info["support"], info["beta"], info["ngrid_x"], info["nplanes"], info["dw"]) == (
+        op.W, op.beta, op.ngx, op.nplanes, op.dw)
+
+
+def test_planner_chooses_oversampling_by_cost():
+    """With sigma 0 the planner weighs gridding work (W^3 per item) against
+    per-plane transform work: a wide field with few visibilities and many
+    w-planes takes the smallest oversampling, a dense narrow field (the
+    LOW-like workload) keeps sigma 2 and the library's own transforms; an
+    explicit sigma is kept."""
+    from rascil_gb300.wgridder import plan_geometry
+    wide = plan_geometry(2048, 2048, 5.8e-4, 5.8e-4, 1e-5, True, -700.0, 700.0, nrows=100000,
+                         nchan=2, precision="fp32")
+    assert wide["sigma"] == 1.25 and wide["fft_mode"] == 1
+    dense = plan_geometry(8192, 8192, 1e-5, 1e-5, 1e-5, True, -40000.0, 41000.0,
+                          nrows=16744448, nchan=16, npol=4, precision="fp32")
+    assert dense["sigma"] == 2.0 and dense["fft_mode"] == 2
+    fixed = plan_geometry(2048, 2048, 5.8e-4, 5.8e-4, 1e-5, True, -700.0, 700.0, nrows=100000,
+                          nchan=2, precision="fp32", sigma=2.0)
+    assert fixed["sigma"] == 2.0

@@ -18,7 +18,7 @@ def test_choose_record_and_reload(tmp_path, monkeypatch):
     monkeypatch.setattr(tuning, "_loaded", [False])
     assert tuning.choose(key, 512, 512, 129024, 1) == {"sigma": 1.5, "tile": 16, "slab": 2}
     tuning.forget(key)
-    assert tuning.choose(key, 512, 512, 129024, 1)["sigma"] == 2.0
+    assert tuning.choose(key, 512, 512, 129024, 1)["sigma"] == 0.0
 
 
 def test_corrupt_cache_is_ignored(tmp_path, monkeypatch):
@@ -29,4 +29,4 @@ def test_corrupt_cache_is_ignored(tmp_path, monkeypatch):
     monkeypatch.setattr(tuning, "_mem", {})
     monkeypatch.setattr(tuning, "_loaded", [False])
     key = tuning.shape_key(64, 64, 1e-3, 1, "fp32", 1e-5, True, 10, 1)
-    assert tuning.choose(key, 64, 64, 10, 1)["sigma"] == 2.0
+    assert tuning.choose(key, 64, 64, 10, 1)["sigma"] == 0.0

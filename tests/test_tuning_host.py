@@ -24,7 +24,7 @@ def _fresh(t):
 
 def test_defaults_then_recorded_choice(tuning):
     key = tuning.shape_key(8192, 8192, 1e-5, 4, "fp32", 1e-5, True, 16744448, 16)
-    assert tuning.choose(key, 8192, 8192, 16744448, 16) == {"sigma": 2.0, "tile": 32, "slab": 4}
+    assert tuning.choose(key, 8192, 8192, 16744448, 16) == {"sigma": 0.0, "tile": 0, "slab": 0}
     tuning.record(key, {"sigma": 1.75, "tile": 16, "slab": 2}, {"a": 1.0})
     assert tuning.choose(key, 8192, 8192, 1, 1) == {"sigma": 1.75, "tile": 16, "slab": 2}
     # served from the file after the in-memory state is gone
@@ -34,7 +34,7 @@ def test_defaults_then_recorded_choice(tuning):
     assert data["version"] == 1 and data["entries"][key]["timings"] == {"a": 1.0}
     tuning.forget(key)
     _fresh(tuning)
-    assert tuning.choose(key, 8192, 8192, 1, 1)["sigma"] == 2.0
+    assert tuning.choose(key, 8192, 8192, 1, 1)["sigma"] == 0.0
 
 
 def test_shape_key_separates_what_changes_the_choice(tuning):
@@ -53,7 +53,7 @@ def test_shape_key_separates_what_changes_the_choice(tuning):
 def test_corrupt_or_foreign_cache_files_are_ignored(tuning, content):
     with open(tuning.cache_path(), "w") as f:
         f.write(content)
-    assert tuning.choose("k", 256, 256, 1, 1) == {"sigma": 2.0, "tile": 32, "slab": 4}
+    assert tuning.choose("k", 256, 256, 1, 1) == {"sigma": 0.0, "tile": 0, "slab": 0}
 
 
 def test_concurrent_records_are_all_kept(tuning):
