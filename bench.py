@@ -104,6 +104,7 @@ def parse():
                          "reference's own CUDA kernel")
     ap.add_argument("--gd-steps", type=int, default=200)
     ap.add_argument("--nsnap", type=int, default=256)
+    ap.add_argument("--nslots", type=int, default=8)
     ap.add_argument("--e2e-gd-steps", type=int, default=20)
     return ap.parse_args()
 
@@ -1318,24 +1319,33 @@ def bench_batch(args):
     nvis = sum(r["nvis"] for r in raw)
     eps = 1e-5
 
-    def one_by_one():
+    def one_by_one(sigma):
         for i, sn in enumerate(snaps):
             p = Plan(sn["uvw"], sn["freq"], sn["npix"], sn["npix"], sn["cell"], sn["cell"], eps,
-                     True, precision="fp32", grid_budget_bytes=2 << 30)
+                     True, precision="fp32", grid_budget_bytes=2 << 30, sigma=sigma)
             p.ms2dirty(vis[i], layout="yx")
             p.dirty2ms(models[i], layout="yx")
             p.close()
 
-    def batched():
-        b = SnapshotBatch(snaps, eps, precision="fp32", nslots=8)
-        b.run(vis, models)
-        b.close()
-
+    t0 = time.perf_counter()
+    b = SnapshotBatch(snaps, eps, precision="fp32", nslots=args.nslots)
+    torch.cuda.synchronize()
+    plan_s = time.perf_counter() - t0
+    sigmas = sorted({p.info["sigma"] for p in b.plans})
     sampler = ClockSampler(device.index)
-    ms_batch, clocks, stats = _event_loop(batched, args.steps, args.warmup, sampler)
-    ms_seq, _, _ = _event_loop(one_by_one, 1, 1, profile=False)
+    # the device program: per round one persistent gridding and one degridding
+    # launch over every slot's snapshot (device work queue)
+    ms_batch, clocks, stats = _event_loop(lambda: b.run_native(vis, models), args.steps,
+                                          args.warmup, sampler)
+    ms_loop, _, _ = _event_loop(lambda: b.run(vis, models), args.steps, 1, profile=False)
+    b.capture(vis, models)
+    ms_graph, _, _ = _event_loop(b.replay, args.steps, 1, profile=False)
+    b.close()
+    ms_seq, _, _ = _event_loop(lambda: one_by_one(0.0), 1, 1, profile=False)
+    ms_seq2, _, _ = _event_loop(lambda: one_by_one(2.0), 1, 1, profile=False)
     launches = sum(v["launches"] for k, v in stats.items() if not k.startswith("cufft"))
     roof, kernels = roofline(stats, load_peaks())
+    rate = lambda ms: round(2 * nvis / (ms * 1e-3) / 1e6, 2)  # noqa: E731
     # CPU baseline: the oracle's C gridder on a sample of snapshots (host only)
     from oracle import cgridder
     rng = numpy.random.default_rng(1)
@@ -1361,8 +1371,20 @@ def bench_batch(args):
     return _aux_line(args, "Mvis/s invert+predict over 256 uneven snapshots on 1 GB300",
                      2 * nvis / (ms_batch * 1e-3) / 1e6, "Mvis/s", ms_batch, workload, roof,
                      kernels, clocks, int(launches / args.steps), dtype="f32",
-                     one_plan_per_snapshot={"ms": round(ms_seq, 1),
-                                            "value": round(2 * nvis / (ms_seq * 1e-3) / 1e6, 2)},
+                     program="gb_batch_run: pre-planned snapshots on %d slots, per round one "
+                             "persistent gridding and one degridding launch over every slot's "
+                             "snapshot (device work queue), transforms on the slot streams"
+                             % args.nslots,
+                     planner_sigmas=sigmas, plan_creation_s=round(plan_s, 3),
+                     graph_replay={"ms": round(ms_graph, 1), "value": rate(ms_graph)},
+                     per_snapshot_calls_on_slot_streams={"ms": round(ms_loop, 1),
+                                                         "value": rate(ms_loop)},
+                     one_plan_per_snapshot={"ms": round(ms_seq, 1), "value": rate(ms_seq),
+                                            "note": "plan + invert + predict per snapshot on "
+                                                    "one stream, planner's oversampling, plan "
+                                                    "creation included"},
+                     one_plan_per_snapshot_sigma2={"ms": round(ms_seq2, 1),
+                                                   "value": rate(ms_seq2)},
                      cpu_baseline={"value": round(2 * cpu_v / cpu_t / 1e6, 4), "unit": "Mvis/s",
                                    "cores": cgridder.max_threads(), "kind": "port",
                                    "sample": "oracle C gridder (FP64) invert + predict of %d "

@@ -4,15 +4,24 @@ RASCIL images a list of visibility blocks by running one invert/predict per
 block through Dask (``rascil/workflows/rsexecute/imaging/imaging_rsexecute.py:
 72-157``).  Here the whole list runs as one device program:
 
-* one plan per snapshot is created up front (its w range and geometry);
-* a fixed pool of workspace slots, each on its own CUDA stream, is reused
-  round-robin, so the small snapshots' sorts, gridding, FFTs and screens
-  overlap instead of running one after another;
-* the complete sequence (bind/sort + invert + predict for every snapshot)
+* one plan per snapshot is created up front (its w range and geometry, the
+  grid oversampling from the planner's cost model: wide-field snapshots with
+  few visibilities take a small oversampling, which cuts their w-plane
+  transform volume several times);
+* a fixed pool of workspace slots, each on its own CUDA stream, serves the
+  snapshots round-robin;
+* :meth:`SnapshotBatch.run_native` issues the list through ``gb_batch_run``:
+  rounds in which the next batch of w-planes of every slot's snapshot is a
+  job, all jobs gridded by ONE persistent launch (and degridded by one)
+  that pulls (snapshot, chunk) work from a device work queue, with each
+  snapshot's transforms on its slot's stream;
+* the complete program (bucket sorts + invert + predict of every snapshot)
   can be captured once as a CUDA graph and replayed with a single launch.
 
-Inputs and outputs are preallocated device tensors so a captured graph can
-be replayed on new data written into the same buffers.
+:meth:`SnapshotBatch.run` is the same list as plain per-snapshot calls on
+the slot streams (the reference for the tests).  Inputs and outputs are
+preallocated device tensors so a captured graph can be replayed on new data
+written into the same buffers.
 """
 import torch
 
@@ -22,19 +31,22 @@ from .wgridder import Plan
 class SnapshotBatch:
     """:param snapshots: list of dicts with device tensors ``uvw`` [R, 3]
     float64 (u, w as ng.py flips them), ``freq`` [C] float64, and ``npix``,
-    ``cell``; :param nslots: concurrent workspace slots / streams."""
+    ``cell``; :param nslots: concurrent workspace slots / streams (at most
+    16); :param sigmas: per-snapshot grid oversampling (None: the planner's
+    choice, or a cached autotuning result, per snapshot)."""
 
     def __init__(self, snapshots, epsilon, precision="fp32", nslots=8, do_wstacking=True,
-                 device="cuda", grid_budget_bytes=2 << 30):
+                 device="cuda", grid_budget_bytes=2 << 30, sigmas=None):
         self.device = torch.device(device)
         self.precision = precision
         self.plans = []
-        for sn in snapshots:
+        for i, sn in enumerate(snapshots):
             self.plans.append(Plan(sn["uvw"], sn["freq"], sn["npix"], sn["npix"], sn["cell"],
                                    sn["cell"], epsilon, do_wstacking, npol=1,
                                    precision=precision, bind=False,
-                                   grid_budget_bytes=grid_budget_bytes))
-        self.nslots = max(1, min(int(nslots), len(self.plans)))
+                                   grid_budget_bytes=grid_budget_bytes,
+                                   sigma=sigmas[i] if sigmas else 0.0))
+        self.nslots = max(1, min(int(nslots), len(self.plans), 16))
         # slot k serves snapshots k, k + nslots, ...; size it for the largest of them
         need = [0] * self.nslots
         for i, p in enumerate(self.plans):
@@ -73,9 +85,11 @@ class SnapshotBatch:
                 main.wait_stream(s)
 
     def run_native(self, vis, models):
-        """run(vis, models) issued by the library in one call
-        (``gb_batch_run``): the same plans, slots and streams, without a
-        Python round trip per snapshot."""
+        """run(vis, models) as one device program (``gb_batch_run``): rounds
+        over the slots' current snapshots, each round's gridding and
+        degridding of every snapshot in one persistent launch fed from a
+        device work queue, the transforms on the slot streams; no Python
+        round trip per snapshot."""
         import ctypes
 
         from . import _lib
@@ -111,13 +125,15 @@ class SnapshotBatch:
         for s in self.streams:
             main.wait_stream(s)
 
-    def capture(self, vis, models):
-        """Record run(vis, models) as a CUDA graph; replay() re-runs it."""
-        self.run(vis, models)  # warm-up outside capture (cuFFT, caches)
+    def capture(self, vis, models, native=True):
+        """Record run_native(vis, models) (or run() with native=False) as a
+        CUDA graph; replay() re-runs it."""
+        fn = self.run_native if native else self.run
+        fn(vis, models)  # warm-up outside capture (cuFFT, caches)
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.run(vis, models)
+            fn(vis, models)
         self.graph = g
         self._keep = (vis, models)
         return g

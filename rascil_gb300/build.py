@@ -23,7 +23,7 @@ BUILDDIR = os.path.join(HERE, "lib", "obj")
 LIBNAME = "librascil_gb300.so"
 SOURCES = ["gb_plan.cu", "gb_invert.cu", "gb_predict.cu", "gb_capi.cu", "gb_dft.cu", "gb_profile.cu",
            "gb_noalloc.cu", "gb_gains.cu", "gb_fft.cu", "gb_weight.cu",
-           "gb_rotate.cu"]
+           "gb_rotate.cu", "gb_batch.cu"]
 HEADERS = ["gb_internal.cuh", "gb_plan.cuh", "gb_profile.cuh", "gb_fft.cuh", "gb_async.cuh", "es_table.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo",

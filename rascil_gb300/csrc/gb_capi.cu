@@ -166,44 +166,4 @@ int gb_dirty2ms(const double *uvw, const double *freq, int64_t nrows, int32_t nc
                  pixsize_y, epsilon, do_wstacking, precision, ms, stream);
 }
 
-int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
-                 const size_t *workspace_bytes, void *const *streams, int32_t nslots,
-                 const void *const *vis, void *const *dirty, const void *const *model,
-                 void *const *pred, int32_t layout) {
-  if (nplans < 0 || (nplans > 0 && (!plans || !workspaces || !workspace_bytes || !streams)) ||
-      nslots < 1) {
-    set_error("gb_batch_run: NULL array or no slot");
-    return GB_ERR_INVALID_ARG;
-  }
-  for (int32_t i = 0; i < nplans; ++i) {
-    gb_plan *p = plans[i];
-    const int32_t k = i % nslots;
-    if (!p) {
-      set_error("gb_batch_run: plan %d is NULL", (int)i);
-      return GB_ERR_INVALID_ARG;
-    }
-    int rc = gb_plan_bind(p, workspaces[k], workspace_bytes[k], streams[k]);
-    if (rc) return rc;
-    const int32_t np = p->g.NP;
-    if (vis && vis[i]) {
-      if (!dirty || !dirty[i]) {
-        set_error("gb_batch_run: plan %d has visibilities but no dirty image", (int)i);
-        return GB_ERR_INVALID_ARG;
-      }
-      rc = gb_plan_ms2dirty(p, vis[i], np, nullptr, nullptr, GB_FLAGS_NONE, nullptr, 0, dirty[i],
-                            layout, nullptr, streams[k]);
-      if (rc) return rc;
-    }
-    if (model && model[i]) {
-      if (!pred || !pred[i]) {
-        set_error("gb_batch_run: plan %d has a model but no output visibilities", (int)i);
-        return GB_ERR_INVALID_ARG;
-      }
-      rc = gb_plan_dirty2ms(p, model[i], layout, nullptr, nullptr, np, pred[i], streams[k]);
-      if (rc) return rc;
-    }
-  }
-  return GB_OK;
-}
-
 }  // extern "C"

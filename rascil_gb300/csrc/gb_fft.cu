@@ -205,6 +205,29 @@ __device__ __forceinline__ void screen_sincos(ulonglong2 ad, int k, float *sn, f
   sincospif((float)hi * 0x1p-31f, sn, cs);
 }
 
+// The screens of planes b0, b0 + 1, ... at one pixel by rotation: (cs, sn)
+// of plane b0 from its exact fixed-point phase, then one complex multiply
+// by exp(2 pi i D) per plane (an error of a few FP32 roundings per plane
+// step; the batches hold a handful of planes), instead of a sincos per plane.
+struct ScreenRot {
+  float cs, sn, dc, ds;
+  __device__ __forceinline__ void start(ulonglong2 ad, int k) {
+    screen_sincos(ad, k, &sn, &cs);
+    screen_sincos(make_ulonglong2(ad.y, 0ull), 0, &ds, &dc);
+  }
+  __device__ __forceinline__ void unit() {
+    cs = 1.f;
+    sn = 0.f;
+    dc = 1.f;
+    ds = 0.f;
+  }
+  __device__ __forceinline__ void next() {
+    const float c = cs * dc - sn * ds, s = sn * dc + cs * ds;
+    cs = c;
+    sn = s;
+  }
+};
+
 // ----------------------------------------------------------------------
 // invert step A: in place, one CTA per (column tile, q2, plane-pol).
 template <int N1>
@@ -304,13 +327,18 @@ __global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 2)
     for (int e = 0; e < NK; ++e)
       sacc[slot(pol, e)] = (first || !ok) ? 0.f : acc[pol * npix + pixel(e)];
   int s = 0;
-  for (int j = 0; j < nb; ++j) {
-    float sn[NK], cs[NK];
+  ScreenRot scr[NK];
 #pragma unroll
-    for (int e = 0; e < NK; ++e) {
-      sn[e] = 0.f;
-      cs[e] = 1.f;
-      if (do_w && ok) screen_sincos(screen[pixel(e)], b0 + j, &sn[e], &cs[e]);
+  for (int e = 0; e < NK; ++e) {
+    if (do_w && ok)
+      scr[e].start(screen[pixel(e)], b0);
+    else
+      scr[e].unit();
+  }
+  for (int j = 0; j < nb; ++j) {
+    if (j > 0) {
+#pragma unroll
+      for (int e = 0; e < NK; ++e) scr[e].next();
     }
 #pragma unroll 1
     for (int pol = 0; pol < NP; ++pol, ++s) {
@@ -325,7 +353,7 @@ __global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 2)
 #pragma unroll
       for (int e = 0; e < NK; ++e) {
         const float2 v = y[e / KK][KL + e % KK];
-        sacc[slot(pol, e)] += v.x * cs[e] + v.y * sn[e];  // Re(v exp(-i theta))
+        sacc[slot(pol, e)] += v.x * scr[e].cs + v.y * scr[e].sn;  // Re(v exp(-i theta))
       }
       __syncthreads();  // tile s consumed before its buffer is refilled
       if (s_abort) {
@@ -348,7 +376,8 @@ __global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 2)
 // predict step A from the corrected image: one CTA per (column tile, q2);
 // loops over the batch's planes and the pols.  The image values (inputs
 // m in [M/4, 3M/4) of each thread) and each plane's screens sit in
-// per-thread shared-memory slots.
+// per-thread shared-memory slots; the screens of the batch's later planes
+// come from the first by rotation (ScreenRot).
 template <int N1, int NP>
 __global__ void __launch_bounds__(ColShape<N1>::THREADS, 2)
     k_cols_a_pred(const ColGeom cg, const float2 *__restrict__ twn, const float *__restrict__ img,
@@ -360,7 +389,8 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS, 2)
   float2 *xb = smem, *tw = smem + N1 * kCW;
   float2 *st = tw + N1;                                  // exp(-2 pi i q2 o / n), o < N1
   float2 *scr = st + N1;                                 // [MK][T][kCW] (cos, sin)
-  float *sv = reinterpret_cast<float *>(scr + MK * T * kCW);  // [NP][MK][T][kCW]
+  float2 *rot = scr + MK * T * kCW;                      // [MK][T][kCW] exp(2 pi i D)
+  float *sv = reinterpret_cast<float *>(rot + MK * T * kCW);  // [NP][MK][T][kCW]
   const int c = threadIdx.x % kCW, t = threadIdx.x / kCW;
   const int p = cg.ox + blockIdx.x * kCW + c;
   const bool ok = p < cg.ox + cg.nx;
@@ -384,9 +414,22 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS, 2)
   for (int j = 0; j < nb; ++j) {
 #pragma unroll
     for (int mm = 0; mm < MK; ++mm) {
-      float sn = 0.f, cs = 1.f;
-      if (do_w && ok) screen_sincos(screen[pixel(mm)], b0 + j, &sn, &cs);
-      scr[slot(mm)] = make_float2(cs, sn);
+      // plane b0 from the fixed-point phase, later planes by rotation
+      ScreenRot r;
+      if (!(do_w && ok)) {
+        r.unit();
+      } else if (j == 0) {
+        r.start(screen[pixel(mm)], b0);
+        rot[slot(mm)] = make_float2(r.dc, r.ds);
+      } else {
+        const float2 e = scr[slot(mm)], d = rot[slot(mm)];
+        r.cs = e.x;
+        r.sn = e.y;
+        r.dc = d.x;
+        r.ds = d.y;
+        r.next();
+      }
+      scr[slot(mm)] = make_float2(r.cs, r.sn);
     }
 #pragma unroll 1
     for (int pol = 0; pol < NP; ++pol) {
@@ -651,7 +694,7 @@ template <int N> constexpr size_t smem_one() { return sizeof(float2) * ((size_t)
 // + screen slots and image slots (N/2 inputs per column)
 template <int N, int NP> constexpr size_t smem_a_pred() {
   return smem_one<N>() + sizeof(float2) * N +
-         (sizeof(float2) + sizeof(float) * NP) * (size_t)(N / 2) * kCW;
+         (2 * sizeof(float2) + sizeof(float) * NP) * (size_t)(N / 2) * kCW;
 }
 // two tile buffers + twiddles + accumulator slots (N/2 kept outputs per column)
 template <int N, int NP> constexpr size_t smem_b_inv() {

@@ -23,16 +23,6 @@ struct ColGeom {
   }
 };
 
-// Row order of a predict grid after the column transforms: logical row
-// q = k1 + N1 k2 sits at physical row N2 k1 + k2 = ((q & (N1-1)) << s2) |
-// (q >> s1).  s1 < 0: natural order.
-struct RowPerm {
-  int s1, s2;
-  __host__ __device__ __forceinline__ int row(int q) const {
-    return s1 < 0 ? q : (((q & ((1 << s1) - 1)) << s2) | (q >> s1));
-  }
-};
-
 // True when a column of length n has a supported split n = N1 N2
 // (power of two, 256 <= n <= 32768; N1 <= 128, N2 <= 256).
 bool column_split(int n, int &N1, int &N2);

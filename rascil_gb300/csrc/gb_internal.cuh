@@ -311,6 +311,16 @@ struct LaneMap {
   __device__ __forceinline__ int pol(int i) const { return p0 + i * G; }
 };
 
+// Row order of a predict grid after the column transforms: logical row
+// q = k1 + N1 k2 sits at physical row N2 k1 + k2 = ((q & (N1-1)) << s2) |
+// (q >> s1).  s1 < 0: natural order.
+struct RowPerm {
+  int s1, s2;
+  __host__ __device__ __forceinline__ int row(int q) const {
+    return s1 < 0 ? q : (((q & ((1 << s1) - 1)) << s2) | (q >> s1));
+  }
+};
+
 // Error reporting -------------------------------------------------------
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);

@@ -156,26 +156,36 @@ __device__ __forceinline__ void fixed_add(long long *p, long long v) {
   atomicAdd(reinterpret_cast<unsigned long long *>(p), static_cast<unsigned long long>(v));
 }
 
+// Shared memory of the tile gridder: the fixed-point sub-grid (2 NP planes
+// of the plan's tile layout), then, in the FP32 form, the per-chunk cache of
+// every item's kernel values {loc, ku[W], kv[W], kw[W]} and scaled values.
+template <typename R> struct GridSmem;
+template <> struct GridSmem<float> {
+  static constexpr bool kCache = true;
+};
+template <> struct GridSmem<double> {
+  static constexpr bool kCache = false;
+};
+
+// Grid one work chunk (up to kChunkItems items of one (w-slab, uv tile)
+// bucket) into the planes [b0, b0 + nb) of `grid`: spread every item over
+// its W x W support in the shared sub-grid, plane by plane, then flush the
+// sub-grid to HBM with float2 atomics and leave it zeroed.  `acc` must be all
+// zero on entry (it is on exit); kc / cc are the FP32 item cache; s_red and
+// s_scale are block-shared scratch.  Every thread of the block calls it.
 template <typename R, int NP, int AW>
-__global__ void __launch_bounds__(kThreads)
-    k_grid(const Geom g, const typename Traits<R>::Item *__restrict__ items,
-           const typename Traits<R>::C *__restrict__ cvis, const Chunk *__restrict__ chunks,
-           const uint32_t *__restrict__ chunk_off, int b0, int nb,
-           typename Traits<R>::C *__restrict__ grid, uint32_t *__restrict__ counter) {
+__device__ __forceinline__ void grid_chunk(
+    const Geom &g, const typename Traits<R>::Item *__restrict__ items,
+    const typename Traits<R>::C *__restrict__ cvis, const Chunk ch, int b0, int nb,
+    typename Traits<R>::C *__restrict__ grid, typename FixedAcc<R>::T *acc, R *kc,
+    typename Traits<R>::C *cc, double *s_red, R *s_scale) {
   using C = typename Traits<R>::C;
   using A = typename FixedAcc<R>::T;
   using LM = LaneMap<NP, AW>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  A *acc = reinterpret_cast<A *>(smem_raw);  // [re pols | im pols][SW][pitch]
+  constexpr bool kCache = GridSmem<R>::kCache;
   const int W = g.W, T = g.T;
   const TileLayout L = tile_layout(T, W, NP);
-  // FP32: per-chunk cache of every item's kernel values {loc, ku[W], kv[W],
-  // kw[W]} and scaled gridded values, computed once per chunk instead of
-  // once per item and plane
-  constexpr bool kCache = std::is_same<R, float>::value;
   const int KS = 3 * W + 1;
-  R *kc = reinterpret_cast<R *>(acc + 2 * NP * L.plane);     // [kChunkItems][KS]
-  C *cc = reinterpret_cast<C *>(kc + kChunkItems * KS);      // [kChunkItems][NP]
   const int SW = L.SW, SW2 = SW * SW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const LM lm(lane);
@@ -183,20 +193,7 @@ __global__ void __launch_bounds__(kThreads)
   const R beta = (R)g.beta;
   const int ntiles = g.ntu * g.ntv;
   const size_t plane = (size_t)g.ngx * g.ngy;
-  int s_lo, s_hi;
-  batch_slabs(g, b0, nb, s_lo, s_hi);
-  const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
-  const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
-  for (int i = threadIdx.x; i < 2 * NP * L.plane; i += kThreads) acc[i] = 0;
-  __shared__ uint32_t s_ci;
-  __shared__ double s_red[kWarps];
-  __shared__ R s_scale[2];
-  for (;;) {
-    if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
-    __syncthreads();
-    const uint32_t ci = s_ci;
-    if (ci >= c_end) break;
-    const Chunk ch = chunks[ci];
+  {
     const int slab = (int)(ch.bucket / (uint32_t)ntiles);
     const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
     const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
@@ -298,30 +295,37 @@ __global__ void __launch_bounds__(kThreads)
           }
         }
         const int lu = (int)(loc & 0xffu), lv = (int)((loc >> 8) & 0xffu);
+        // the lane's column kernel value folded into its values once per
+        // item and plane: a support row then costs one multiply per part
+#pragma unroll
+        for (int i = 0; i < LM::NPL; ++i) {
+          c[i].x *= ku;
+          c[i].y *= ku;
+        }
         constexpr int kMaxRows = (AW + LM::RS - 1) / LM::RS;  // W <= AW: unrolled, predicated
+        const int cell0 = (lv + lm.r0) * L.pitch + lu + lm.a;
 #pragma unroll
         for (int r = 0; r < kMaxRows; ++r) {
           const int b = lm.r0 + r * LM::RS;
           const R kv = __shfl_sync(0xffffffffu, kv_lane, 16 + min(b, W - 1));
           if (b < W && lm.a < W) {
-            const R kk = ku * kv;
             if (direct) {
               int p = tu * T + lu + lm.a;
               if (p >= g.ngx) p -= g.ngx;
               int q = tv * T + lv + b;
               if (q >= g.ngy) q -= g.ngy;
-              const R f = ((p + q) & 1) ? -kk : kk;
+              const R f = ((p + q) & 1) ? -kv : kv;
 #pragma unroll
               for (int i = 0; i < LM::NPL; ++i)
                 grid_add(&gplane[lm.pol(i) * plane + (size_t)q * g.ngx + p], f * c[i].x,
                          f * c[i].y);
             } else {
-              const int cell = (lv + b) * L.pitch + lu + lm.a;
+              const int cell = cell0 + r * LM::RS * L.pitch;
 #pragma unroll
               for (int i = 0; i < LM::NPL; ++i) {
                 const int pl = lm.pol(i);
-                fixed_add(&acc[pl * L.plane + cell], to_fixed(kk * c[i].x));
-                fixed_add(&acc[(NP + pl) * L.plane + cell], to_fixed(kk * c[i].y));
+                fixed_add(&acc[pl * L.plane + cell], to_fixed(kv * c[i].x));
+                fixed_add(&acc[(NP + pl) * L.plane + cell], to_fixed(kv * c[i].y));
               }
             }
           }
@@ -351,6 +355,37 @@ __global__ void __launch_bounds__(kThreads)
         __syncthreads();
       }
     }
+  }
+}
+
+template <typename R, int NP, int AW>
+__global__ void __launch_bounds__(kThreads)
+    k_grid(const Geom g, const typename Traits<R>::Item *__restrict__ items,
+           const typename Traits<R>::C *__restrict__ cvis, const Chunk *__restrict__ chunks,
+           const uint32_t *__restrict__ chunk_off, int b0, int nb,
+           typename Traits<R>::C *__restrict__ grid, uint32_t *__restrict__ counter) {
+  using C = typename Traits<R>::C;
+  using A = typename FixedAcc<R>::T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  A *acc = reinterpret_cast<A *>(smem_raw);  // [re pols | im pols][SW][pitch]
+  const TileLayout L = tile_layout(g.T, g.W, NP);
+  R *kc = reinterpret_cast<R *>(acc + 2 * NP * L.plane);     // [kChunkItems][3 W + 1]
+  C *cc = reinterpret_cast<C *>(kc + kChunkItems * (3 * g.W + 1));  // [kChunkItems][NP]
+  const int ntiles = g.ntu * g.ntv;
+  int s_lo, s_hi;
+  batch_slabs(g, b0, nb, s_lo, s_hi);
+  const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
+  const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
+  for (int i = threadIdx.x; i < 2 * NP * L.plane; i += kThreads) acc[i] = 0;
+  __shared__ uint32_t s_ci;
+  __shared__ double s_red[kWarps];
+  __shared__ R s_scale[2];
+  for (;;) {
+    if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t ci = s_ci;
+    if (ci >= c_end) break;
+    grid_chunk<R, NP, AW>(g, items, cvis, chunks[ci], b0, nb, grid, acc, kc, cc, s_red, s_scale);
   }
 }
 
@@ -466,106 +501,318 @@ size_t grid_smem_bytes(const gb_plan *p) {
   return b;
 }
 
+// The invert driver in steps (a batch of plans interleaves them across
+// plans: gb_batch.cu).  begin: per-item values; per w-plane batch bi: zero,
+// grid, transform (+ screen and accumulation); end: correction and layout.
 template <typename R, int NP>
-static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
-                         const void *flags, int ftype, const PolMat &pm, int psf, void *dirty,
-                         int layout, double *sumwt, cudaStream_t s) {
+static int inv_begin_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
+                          const void *flags, int ftype, const PolMat &pm, int psf, double *sumwt,
+                          cudaStream_t s) {
+  using C = typename Traits<R>::C;
+  using Item = typename Traits<R>::Item;
+  const Geom &g = p->g;
+  char *tmp = p->ws + p->off_temp;
+  C *cvis = reinterpret_cast<C *>(tmp + p->c_cvis);
+  uint32_t *counters = p->at<uint32_t>(p->off_counters);
+  const Item *items = p->at<Item>(p->off_items);
+  GB_CUDA(cudaMemsetAsync(counters, 0, 4 * (size_t)p->nbatches, s));
+  if (sumwt) GB_CUDA(cudaMemsetAsync(sumwt, 0, sizeof(double) * NP, s));
+  const unsigned item_blocks = (unsigned)std::min<int64_t>(
+      ((int64_t)g.nitems + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
+  const double fb = ftype == GB_FLAGS_I64 ? 8.0 : (ftype == GB_FLAGS_U8 ? 1.0 : 0.0);
+  const double per = sizeof(Item) + (psf ? 0.0 : npv * sizeof(C)) +
+                     (wgt ? NP * sizeof(R) : 0.0) + npv * fb + NP * sizeof(C);
+  ProfScope ps(kProfPrepVis, s, per * (double)g.nitems);
+  k_prep_vis<R, NP><<<item_blocks, kThreads, 0, s>>>(
+      g, items, reinterpret_cast<const C *>(vis), npv, reinterpret_cast<const R *>(wgt), flags,
+      ftype, pm, psf, psf && g.shifted ? p->at<const double>(p->off_coords) : nullptr, cvis,
+      sumwt);
+  GB_LAUNCH_CHECK("k_prep_vis");
+  return GB_OK;
+}
+
+template <typename R, int NP>
+static int inv_zero_impl(gb_plan *p, int bi, cudaStream_t s) {
+  using C = typename Traits<R>::C;
+  const Geom &g = p->g;
+  C *grid = reinterpret_cast<C *>(p->ws + p->off_temp + p->c_grid);
+  const int b0 = bi * g.B, nb = std::min(g.B, g.nplanes - b0);
+  const double gbytes = (double)sizeof(C) * nb * NP * (double)g.ngx * g.ngy;
+  if (p->col_fft) {  // only rows the gridder writes; column step A skips the rest
+    ProfScope ps(kProfGridZero, s, p->used_rows(b0, nb) * gbytes);
+    return run_zero_rows(p, grid, b0, nb, s);
+  }
+  ProfScope ps(kProfGridZero, s, gbytes);
+  GB_CUDA(cudaMemsetAsync(grid, 0, (size_t)gbytes, s));
+  return GB_OK;
+}
+
+// Algorithmic bytes and updates of gridding batch bi (profiling).
+template <typename R, int NP>
+static void grid_counts(const gb_plan *p, int bi, double *bytes, double *updates) {
+  using C = typename Traits<R>::C;
+  using Item = typename Traits<R>::Item;
+  const Geom &g = p->g;
+  const int b0 = bi * g.B, nb = std::min(g.B, g.nplanes - b0);
+  const double gbytes = (double)sizeof(C) * nb * NP * (double)g.ngx * g.ngy;
+  // items and their gridded values read once; every grid cell of the
+  // (plane, tile) pairs they reach read and written once (the float2
+  // atomic flush is a read-modify-write), else the rows they reach
+  const double cells = p->touched_cells(b0, nb);
+  const double gmove = cells > 0.0 ? 2.0 * cells * NP * sizeof(C) : p->used_rows(b0, nb) * gbytes;
+  *bytes = (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) + gmove;
+  *updates = p->item_planes(b0, nb) * g.W * g.W * NP;
+}
+
+template <typename R, int NP>
+static int inv_grid_impl(gb_plan *p, int bi, cudaStream_t s) {
   using C = typename Traits<R>::C;
   using Item = typename Traits<R>::Item;
   const Geom &g = p->g;
   char *tmp = p->ws + p->off_temp;
   C *grid = reinterpret_cast<C *>(tmp + p->c_grid);
-  R *acc = reinterpret_cast<R *>(tmp + p->c_img);
-  C *cvis = reinterpret_cast<C *>(tmp + p->c_cvis);
+  const C *cvis = reinterpret_cast<const C *>(tmp + p->c_cvis);
   uint32_t *counters = p->at<uint32_t>(p->off_counters);
   const Item *items = p->at<Item>(p->off_items);
   const Chunk *chunks = p->at<Chunk>(p->off_chunks);
   const uint32_t *chunk_off = p->at<uint32_t>(p->off_chunk_off);
-  const R *corr = p->at<R>(p->off_corr);
-  GB_CUDA(cudaMemsetAsync(counters, 0, 4 * (size_t)p->nbatches, s));
-  if (sumwt) GB_CUDA(cudaMemsetAsync(sumwt, 0, sizeof(double) * NP, s));
-  const unsigned item_blocks = (unsigned)std::min<int64_t>(
-      ((int64_t)g.nitems + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
-  {
-    const double fb = ftype == GB_FLAGS_I64 ? 8.0 : (ftype == GB_FLAGS_U8 ? 1.0 : 0.0);
-    const double per = sizeof(Item) + (psf ? 0.0 : npv * sizeof(C)) +
-                       (wgt ? NP * sizeof(R) : 0.0) + npv * fb + NP * sizeof(C);
-    ProfScope ps(kProfPrepVis, s, per * (double)g.nitems);
-    k_prep_vis<R, NP><<<item_blocks, kThreads, 0, s>>>(
-        g, items, reinterpret_cast<const C *>(vis), npv, reinterpret_cast<const R *>(wgt), flags,
-        ftype, pm, psf,
-        psf && g.shifted ? p->at<const double>(p->off_coords) : nullptr, cvis, sumwt);
-    GB_LAUNCH_CHECK("k_prep_vis");
-  }
-  const size_t plane = (size_t)g.ngx * g.ngy;
+  const int b0 = bi * g.B, nb = std::min(g.B, g.nplanes - b0);
+  const size_t smem = grid_smem_bytes(p);
+  double bytes = 0.0, updates = 0.0;
+  if (prof_on()) grid_counts<R, NP>(p, bi, &bytes, &updates);
+  ProfScope ps(kProfGrid, s, bytes, updates);
+  if (group_lanes(g.W) == 8)
+    k_grid<R, NP, 8><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks, chunk_off,
+                                                            b0, nb, grid, counters + bi);
+  else
+    k_grid<R, NP, 16><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks, chunk_off,
+                                                             b0, nb, grid, counters + bi);
+  GB_LAUNCH_CHECK("k_grid");
+  return GB_OK;
+}
+
+template <typename R, int NP>
+static int inv_transform_impl(gb_plan *p, int bi, cudaStream_t s) {
+  using C = typename Traits<R>::C;
+  const Geom &g = p->g;
+  char *tmp = p->ws + p->off_temp;
+  C *grid = reinterpret_cast<C *>(tmp + p->c_grid);
+  R *acc = reinterpret_cast<R *>(tmp + p->c_img);
+  const int b0 = bi * g.B, nb = std::min(g.B, g.nplanes - b0);
+  const double gbytes = (double)sizeof(C) * nb * NP * (double)g.ngx * g.ngy;
   const int64_t npix = (int64_t)g.nx * g.ny;
+  int rc;
+  if (p->row_fft) {
+    // used rows: read, image half written
+    ProfScope ps(kProfRowsInv, s, 1.5 * p->used_rows(b0, nb) * gbytes);
+    rc = run_rows(p, grid, b0, nb, 1, s);
+  } else {
+    ProfScope ps(kProfFftInv, s, 2.0 * gbytes);
+    rc = run_fft(p, nb, grid, CUFFT_INVERSE, s);
+  }
+  if (rc) return rc;
+  if constexpr (std::is_same<R, float>::value) {
+    if (p->col_fft)  // rows done; columns + screen + accumulate
+      return run_cols_invert(p, grid, b0, nb, acc, bi == 0, s);
+  }
   const unsigned pix_blocks = (unsigned)std::min<int64_t>((npix + kThreads - 1) / kThreads,
                                                           (int64_t)p->num_sms * 32);
-  const size_t smem = grid_smem_bytes(p);
-  for (int bi = 0; bi < p->nbatches; ++bi) {
-    const int b0 = bi * g.B;
-    const int nb = std::min(g.B, g.nplanes - b0);
-    const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
-    const double used = p->used_rows(b0, nb);  // profiling byte counts only
-    if (p->col_fft) {  // only rows the gridder writes; column step A skips the rest
-      ProfScope ps(kProfGridZero, s, used * gbytes);
-      const int rc = run_zero_rows(p, grid, b0, nb, s);
-      if (rc) return rc;
-    } else {
-      ProfScope ps(kProfGridZero, s, gbytes);
-      GB_CUDA(cudaMemsetAsync(grid, 0, sizeof(C) * (size_t)nb * NP * plane, s));
-    }
-    {
-      // items and their gridded values read once; every grid cell of the
-      // (plane, tile) pairs they reach read and written once (the float2
-      // atomic flush is a read-modify-write), else the rows they reach
-      const double cells = p->touched_cells(b0, nb);
-      const double gmove = cells > 0.0 ? 2.0 * cells * NP * sizeof(C) : used * gbytes;
-      ProfScope ps(kProfGrid, s,
-                   (double)p->batch_items(b0, nb) * (sizeof(Item) + NP * sizeof(C)) + gmove,
-                   p->item_planes(b0, nb) * g.W * g.W * NP);
-      if (group_lanes(g.W) == 8)
-        k_grid<R, NP, 8><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks,
-                                                                chunk_off, b0, nb, grid,
-                                                                counters + bi);
-      else
-        k_grid<R, NP, 16><<<p->grid_blocks, kThreads, smem, s>>>(g, items, cvis, chunks,
-                                                                 chunk_off, b0, nb, grid,
-                                                                 counters + bi);
-      GB_LAUNCH_CHECK("k_grid");
-    }
-    int rc;
-    if (p->row_fft) {
-      ProfScope ps(kProfRowsInv, s, 1.5 * used * gbytes);  // used rows: read, image half written
-      rc = run_rows(p, grid, b0, nb, 1, s);
-    } else {
-      ProfScope ps(kProfFftInv, s, 2.0 * gbytes);
-      rc = run_fft(p, nb, grid, CUFFT_INVERSE, s);
-    }
-    if (rc) return rc;
-    if constexpr (std::is_same<R, float>::value) {
-      if (p->col_fft) {  // rows done; columns + screen + accumulate
-        rc = run_cols_invert(p, grid, b0, nb, acc, bi == 0, s);
-        if (rc) return rc;
-        continue;
-      }
-    }
-    {
-      ProfScope ps(kProfScreenAcc, s,
-                   (double)sizeof(C) * nb * NP * npix + (bi ? 2.0 : 1.0) * sizeof(R) * NP * npix);
-      k_screen_acc<R, NP><<<pix_blocks, kThreads, 0, s>>>(g, grid, b0, nb,
-                                                           p->at<double>(p->off_tprime), acc,
-                                                           bi == 0);
-      GB_LAUNCH_CHECK("k_screen_acc");
-    }
-  }
-  dim3 fb((g.nx + 31) / 32, (g.ny + 31) / 32, NP);
-  {
-    ProfScope ps(kProfFinalize, s, 3.0 * sizeof(R) * NP * (double)npix);
-    k_finalize<R><<<fb, dim3(32, 8), 0, s>>>(g, acc, corr, reinterpret_cast<R *>(dirty), layout);
-    GB_LAUNCH_CHECK("k_finalize");
-  }
+  ProfScope ps(kProfScreenAcc, s,
+               (double)sizeof(C) * nb * NP * npix + (bi ? 2.0 : 1.0) * sizeof(R) * NP * npix);
+  k_screen_acc<R, NP><<<pix_blocks, kThreads, 0, s>>>(g, grid, b0, nb,
+                                                       p->at<double>(p->off_tprime), acc, bi == 0);
+  GB_LAUNCH_CHECK("k_screen_acc");
   return GB_OK;
+}
+
+template <typename R, int NP>
+static int inv_end_impl(gb_plan *p, void *dirty, int layout, cudaStream_t s) {
+  const Geom &g = p->g;
+  const R *acc = reinterpret_cast<const R *>(p->ws + p->off_temp + p->c_img);
+  const R *corr = p->at<R>(p->off_corr);
+  const int64_t npix = (int64_t)g.nx * g.ny;
+  dim3 fb((g.nx + 31) / 32, (g.ny + 31) / 32, NP);
+  ProfScope ps(kProfFinalize, s, 3.0 * sizeof(R) * NP * (double)npix);
+  k_finalize<R><<<fb, dim3(32, 8), 0, s>>>(g, acc, corr, reinterpret_cast<R *>(dirty), layout);
+  GB_LAUNCH_CHECK("k_finalize");
+  return GB_OK;
+}
+
+template <typename R, int NP>
+static int ms2dirty_impl(gb_plan *p, const void *vis, int npv, const void *wgt,
+                         const void *flags, int ftype, const PolMat &pm, int psf, void *dirty,
+                         int layout, double *sumwt, cudaStream_t s) {
+  int rc = inv_begin_impl<R, NP>(p, vis, npv, wgt, flags, ftype, pm, psf, sumwt, s);
+  for (int bi = 0; !rc && bi < p->nbatches; ++bi) {
+    rc = inv_zero_impl<R, NP>(p, bi, s);
+    if (!rc) rc = inv_grid_impl<R, NP>(p, bi, s);
+    if (!rc) rc = inv_transform_impl<R, NP>(p, bi, s);
+  }
+  if (!rc) rc = inv_end_impl<R, NP>(p, dirty, layout, s);
+  return rc;
+}
+
+// Dispatch on (precision, NP) for the step entry points.
+#define GB_INV_DISPATCH(p, CALL)                     \
+  do {                                               \
+    if ((p)->precision == GB_FP64) {                 \
+      switch ((p)->g.NP) {                           \
+        case 1: { using R = double; constexpr int NP = 1; return CALL; } \
+        case 2: { using R = double; constexpr int NP = 2; return CALL; } \
+        default: { using R = double; constexpr int NP = 4; return CALL; } \
+      }                                              \
+    }                                                \
+    switch ((p)->g.NP) {                             \
+      case 1: { using R = float; constexpr int NP = 1; return CALL; } \
+      case 2: { using R = float; constexpr int NP = 2; return CALL; } \
+      default: { using R = float; constexpr int NP = 4; return CALL; } \
+    }                                                \
+  } while (0)
+
+int inv_begin(gb_plan *p, const void *vis, int npv, const void *wgt, const void *flags,
+              int ftype, const PolMat &pm, int psf, double *sumwt, cudaStream_t s) {
+  GB_INV_DISPATCH(p, (inv_begin_impl<R, NP>(p, vis, npv, wgt, flags, ftype, pm, psf, sumwt, s)));
+}
+int inv_zero(gb_plan *p, int bi, cudaStream_t s) {
+  GB_INV_DISPATCH(p, (inv_zero_impl<R, NP>(p, bi, s)));
+}
+int inv_transform(gb_plan *p, int bi, cudaStream_t s) {
+  GB_INV_DISPATCH(p, (inv_transform_impl<R, NP>(p, bi, s)));
+}
+int inv_end(gb_plan *p, void *dirty, int layout, cudaStream_t s) {
+  GB_INV_DISPATCH(p, (inv_end_impl<R, NP>(p, dirty, layout, s)));
+}
+
+// ---------------------------------------------------------------------
+// Many plans' gridding in one persistent launch (FP32 form).  The work
+// queue is the concatenation of every job's chunk range (the chunks of the
+// slabs its batch of w-planes reaches); each CTA takes the next index from
+// one atomic counter, finds its job by the prefix of chunk counts (formed by
+// every CTA at start from the plans' chunk offsets on the device, so the
+// host needs no copy) and grids that chunk into the job's planes.
+template <int NP, int AW>
+__global__ void __launch_bounds__(kThreads)
+    k_grid_jobs(const __grid_constant__ GridJobs jobs, int acc_words, int ks_max,
+                uint32_t *__restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int *acc = reinterpret_cast<int *>(smem_raw);
+  float *kc = reinterpret_cast<float *>(acc + acc_words);
+  float2 *cc = reinterpret_cast<float2 *>(kc + kChunkItems * ks_max);
+  __shared__ uint32_t s_wbeg[kMaxJobs + 1], s_cbeg[kMaxJobs];
+  __shared__ uint32_t s_w;
+  __shared__ int s_j;
+  __shared__ double s_red[kWarps];
+  __shared__ float s_scale[2];
+  if (threadIdx.x == 0) {
+    uint32_t w = 0;
+    for (int j = 0; j < jobs.n; ++j) {
+      const GridJob &jb = jobs.job[j];
+      const int ntiles = jb.g.ntu * jb.g.ntv;
+      int s_lo, s_hi;
+      batch_slabs(jb.g, jb.b0, jb.nb, s_lo, s_hi);
+      const uint32_t c0 = jb.chunk_off[(int64_t)s_lo * ntiles];
+      const uint32_t c1 = jb.chunk_off[(int64_t)(s_hi + 1) * ntiles];
+      s_wbeg[j] = w;
+      s_cbeg[j] = c0;
+      w += c1 > c0 ? c1 - c0 : 0u;
+    }
+    s_wbeg[jobs.n] = w;
+  }
+  for (int i = threadIdx.x; i < acc_words; i += kThreads) acc[i] = 0;
+  __syncthreads();
+  const uint32_t total = s_wbeg[jobs.n];
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t w = atomicAdd(counter, 1u);
+      int j = 0;
+      while (j + 1 < jobs.n && s_wbeg[j + 1] <= w) ++j;
+      s_w = w;
+      s_j = j;
+    }
+    __syncthreads();
+    const uint32_t w = s_w;
+    if (w >= total) break;
+    const GridJob &jb = jobs.job[s_j];
+    const uint32_t ci = s_cbeg[s_j] + (w - s_wbeg[s_j]);
+    grid_chunk<float, NP, AW>(jb.g, reinterpret_cast<const ItemF *>(jb.items),
+                              reinterpret_cast<const float2 *>(jb.cvis), jb.chunks[ci], jb.b0,
+                              jb.nb, reinterpret_cast<float2 *>(jb.grid), acc, kc, cc, s_red,
+                              s_scale);
+  }
+}
+
+// Fill one job of a multi-plan gridding launch from a bound FP32 plan.
+int grid_job(gb_plan *p, int bi, GridJob &jb) {
+  if (p->precision != GB_FP32 || !p->bound || bi < 0 || bi >= p->nbatches) {
+    set_error("grid_job: needs a bound FP32 plan and a batch index in range");
+    return GB_ERR_INVALID_ARG;
+  }
+  char *tmp = p->ws + p->off_temp;
+  jb.g = p->g;
+  jb.items = p->at<ItemF>(p->off_items);
+  jb.cvis = tmp + p->c_cvis;
+  jb.chunks = p->at<Chunk>(p->off_chunks);
+  jb.chunk_off = p->at<uint32_t>(p->off_chunk_off);
+  jb.grid = tmp + p->c_grid;
+  jb.b0 = bi * p->g.B;
+  jb.nb = std::min(p->g.B, p->g.nplanes - jb.b0);
+  return GB_OK;
+}
+
+// One launch over `jobs` (all of one NP and lane width); `counter` must be
+// zero.  Blocks: the occupancy of the largest job's shared memory.
+int launch_grid_jobs(const GridJobs &jobs, int num_sms, uint32_t *counter, double bytes,
+                     double updates, cudaStream_t s) {
+  if (jobs.n < 1 || jobs.n > kMaxJobs) {
+    set_error("launch_grid_jobs: %d jobs (1..%d)", jobs.n, kMaxJobs);
+    return GB_ERR_INVALID_ARG;
+  }
+  const int NP = jobs.job[0].g.NP, AW = group_lanes(jobs.job[0].g.W);
+  int acc_words = 0, ks_max = 0;
+  for (int j = 0; j < jobs.n; ++j) {
+    const Geom &g = jobs.job[j].g;
+    if (g.NP != NP || group_lanes(g.W) != AW) {
+      set_error("launch_grid_jobs: jobs of one launch share NP and lane width");
+      return GB_ERR_INVALID_ARG;
+    }
+    const TileLayout L = tile_layout(g.T, g.W, g.NP);
+    acc_words = std::max(acc_words, 2 * NP * L.plane);
+    ks_max = std::max(ks_max, 3 * g.W + 1);
+  }
+  const size_t smem = (size_t)acc_words * 4 + (size_t)kChunkItems * (ks_max * 4 + NP * 8);
+  ProfScope ps(kProfGrid, s, bytes, updates);
+#define GB_GJ(NPV, AWV)                                                                      \
+  {                                                                                          \
+    auto k = k_grid_jobs<NPV, AWV>;                                                          \
+    GB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+    int per_sm = 0;                                                                          \
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem));      \
+    if (per_sm < 1) {                                                                        \
+      set_error("k_grid_jobs cannot launch with %zu bytes of shared memory", smem);         \
+      return GB_ERR_INVALID_ARG;                                                             \
+    }                                                                                        \
+    k<<<per_sm * num_sms, kThreads, smem, s>>>(jobs, acc_words, ks_max, counter);            \
+  }
+  if (AW == 8) {
+    if (NP == 1) GB_GJ(1, 8) else if (NP == 2) GB_GJ(2, 8) else GB_GJ(4, 8)
+  } else {
+    if (NP == 1) GB_GJ(1, 16) else if (NP == 2) GB_GJ(2, 16) else GB_GJ(4, 16)
+  }
+#undef GB_GJ
+  GB_LAUNCH_CHECK("k_grid_jobs");
+  return GB_OK;
+}
+
+// Profiling counts of gridding batch bi of a plan (0 while profiling is off).
+void grid_job_counts(const gb_plan *p, int bi, double *bytes, double *updates) {
+  *bytes = 0.0;
+  *updates = 0.0;
+  if (!prof_on()) return;
+  switch (p->g.NP) {
+    case 1: grid_counts<float, 1>(p, bi, bytes, updates); break;
+    case 2: grid_counts<float, 2>(p, bi, bytes, updates); break;
+    default: grid_counts<float, 4>(p, bi, bytes, updates); break;
+  }
 }
 
 int run_ms2dirty(gb_plan *p, const void *vis, int npv, const void *wgt, const void *flags,

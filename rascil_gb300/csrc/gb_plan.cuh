@@ -129,6 +129,47 @@ int run_dirty2ms(gb_plan *p, const void *dirty, int layout, const void *wgt,
                  const PolMat &pm, int npv, void *vis, cudaStream_t s);
 int setup_tile_kernels(gb_plan *p);
 
+// The same drivers in steps, for a batch of plans that interleaves them
+// (gb_batch.cu).  Invert: begin, then per w-plane batch bi zero -> grid ->
+// transform, then end.  Predict: begin, then per batch transform -> degrid.
+int inv_begin(gb_plan *p, const void *vis, int npv, const void *wgt, const void *flags,
+              int ftype, const PolMat &pm, int psf, double *sumwt, cudaStream_t s);
+int inv_zero(gb_plan *p, int bi, cudaStream_t s);
+int inv_transform(gb_plan *p, int bi, cudaStream_t s);
+int inv_end(gb_plan *p, void *dirty, int layout, cudaStream_t s);
+int pred_begin(gb_plan *p, const void *dirty, int layout, cudaStream_t s);
+int pred_transform(gb_plan *p, int bi, cudaStream_t s);
+
+// One plan's batch of w-planes in a multi-plan gridding or degridding launch
+// (FP32 form), passed to the kernel by value.
+constexpr int kMaxJobs = 16;
+struct GridJob {
+  Geom g;
+  const void *items;          // ItemF, bucket order
+  const void *cvis;           // gridding: per-item values; degridding: unused
+  const Chunk *chunks;
+  const uint32_t *chunk_off;  // per-bucket chunk offsets (device)
+  void *grid;                 // the batch's planes
+  int b0, nb;                 // the batch's w-planes
+  // degridding only
+  void *vis;                  // [nrows][nchan][npv] complex64 output
+  int npv, pad;
+  const float *wgt;           // or null
+  RowPerm rp;
+};
+struct GridJobs {
+  int n;
+  GridJob job[kMaxJobs];
+};
+int grid_job(gb_plan *p, int bi, GridJob &jb);
+void grid_job_counts(const gb_plan *p, int bi, double *bytes, double *updates);
+int launch_grid_jobs(const GridJobs &jobs, int num_sms, uint32_t *counter, double bytes,
+                     double updates, cudaStream_t s);
+int degrid_job(gb_plan *p, int bi, void *vis, int npv, GridJob &jb);
+void degrid_job_counts(const gb_plan *p, int bi, int npv, double *bytes, double *updates);
+int launch_degrid_jobs(const GridJobs &jobs, const PolMat &pm, int num_sms, uint32_t *counter,
+                       double bytes, double updates, cudaStream_t s);
+
 }  // namespace gb
 
 #define GB_CUDA(call)                                          \

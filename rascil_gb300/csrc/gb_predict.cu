@@ -330,37 +330,27 @@ __host__ __device__ constexpr int lane_row(int NP, int SW) {
 // bank groups instead of the four of one parity.
 // Per item-plane that is W^2 NP shared loads and 2 W^2 NP FMAs with no
 // cross-lane reduction, against the warp-per-item map of k_degrid.
+// Degrid one work chunk (up to kChunkItems items of one bucket, thread i
+// owning item i) over the planes [b0, b0 + nb) of `grid` into vis.  stage /
+// skv: the block's shared staging buffers (2 x [SW][rowf2] float2, then
+// [WT][kThreads] floats).  Every thread of the block calls it; it ends with
+// the staging buffers free.
 template <int NP, int WT>
-__global__ void __launch_bounds__(kThreads, 2)
-    k_degrid_lane(const Geom g, const ItemF *__restrict__ items, const Chunk *__restrict__ chunks,
-                  const uint32_t *__restrict__ chunk_off, int b0, int nb,
-                  const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
-                  const float *__restrict__ wgt, const PolMat pm, const RowPerm rp,
-                  uint32_t *__restrict__ counter) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void degrid_lane_chunk(
+    const Geom &g, const ItemF *__restrict__ items, const Chunk ch, int b0, int nb,
+    const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
+    const float *__restrict__ wgt, const PolMat &pm, const RowPerm &rp, float2 *stage,
+    float *skv) {
   const int T = g.T;
   const int SW = T + WT - 1, rowf2 = lane_row(NP, SW), pstride = SW * rowf2;
-  float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][rowf2]
-  float *skv = reinterpret_cast<float *>(stage + 2 * pstride);   // [WT][kThreads]: own kv
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  (void)lane;
   const float scale_u = 2.f / (float)WT;
   const float beta = (float)g.beta;
   const int ntiles = g.ntu * g.ntv;
   const int64_t plane = (int64_t)g.ngx * g.ngy;
   const int wk = g.do_w ? WT : 1;
-  const int lo = b0 - (g.S + WT - 2);
-  const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
-  const int s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
-  const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
-  const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
-  __shared__ uint32_t s_ci;
-  for (;;) {
-    if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
-    __syncthreads();
-    const uint32_t ci = s_ci;
-    __syncthreads();  // every thread has read s_ci
-    if (ci >= c_end) break;
-    const Chunk ch = chunks[ci];
+  {
     const int slab = (int)(ch.bucket / (uint32_t)ntiles);
     const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
     const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
@@ -522,6 +512,95 @@ __global__ void __launch_bounds__(kThreads, 2)
   }
 }
 
+template <int NP, int WT>
+__global__ void __launch_bounds__(kThreads, 2)
+    k_degrid_lane(const Geom g, const ItemF *__restrict__ items, const Chunk *__restrict__ chunks,
+                  const uint32_t *__restrict__ chunk_off, int b0, int nb,
+                  const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
+                  const float *__restrict__ wgt, const PolMat pm, const RowPerm rp,
+                  uint32_t *__restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int SW = g.T + WT - 1, pstride = SW * lane_row(NP, SW);
+  float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][rowf2]
+  float *skv = reinterpret_cast<float *>(stage + 2 * pstride);   // [WT][kThreads]: own kv
+  const int ntiles = g.ntu * g.ntv;
+  const int lo = b0 - (g.S + WT - 2);
+  const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
+  const int s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
+  const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
+  const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
+  __shared__ uint32_t s_ci;
+  for (;;) {
+    if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t ci = s_ci;
+    __syncthreads();  // every thread has read s_ci
+    if (ci >= c_end) break;
+    degrid_lane_chunk<NP, WT>(g, items, chunks[ci], b0, nb, grid, vis, npv, wgt, pm, rp, stage,
+                              skv);
+  }
+}
+
+// Many plans' degridding in one persistent launch (FP32 form, one support
+// WT): the work queue is the concatenation of every job's chunk range, as
+// in k_grid_jobs; each CTA takes the next index from one atomic counter and
+// degrids that chunk of its job into the job's visibilities.
+template <int NP, int WT>
+__global__ void __launch_bounds__(kThreads, 2)
+    k_degrid_lane_jobs(const __grid_constant__ GridJobs jobs, const PolMat pm,
+                       uint32_t *__restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t s_wbeg[kMaxJobs + 1], s_cbeg[kMaxJobs];
+  __shared__ uint32_t s_w;
+  __shared__ int s_j;
+  int pstride_max = 0;
+  for (int j = 0; j < jobs.n; ++j) {
+    const int SW = jobs.job[j].g.T + WT - 1;
+    pstride_max = max(pstride_max, SW * lane_row(NP, SW));
+  }
+  float2 *stage = reinterpret_cast<float2 *>(smem_raw);
+  float *skv = reinterpret_cast<float *>(stage + 2 * pstride_max);
+  if (threadIdx.x == 0) {
+    uint32_t w = 0;
+    for (int j = 0; j < jobs.n; ++j) {
+      const GridJob &jb = jobs.job[j];
+      const Geom &g = jb.g;
+      const int ntiles = g.ntu * g.ntv;
+      const int lo = jb.b0 - (g.S + WT - 2);
+      const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
+      const int s_hi = min(g.nslabs - 1, (jb.b0 + jb.nb - 1) / g.S);
+      const uint32_t c0 = jb.chunk_off[(int64_t)s_lo * ntiles];
+      const uint32_t c1 = jb.chunk_off[(int64_t)(s_hi + 1) * ntiles];
+      s_wbeg[j] = w;
+      s_cbeg[j] = c0;
+      w += c1 > c0 ? c1 - c0 : 0u;
+    }
+    s_wbeg[jobs.n] = w;
+  }
+  __syncthreads();
+  const uint32_t total = s_wbeg[jobs.n];
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const uint32_t w = atomicAdd(counter, 1u);
+      int j = 0;
+      while (j + 1 < jobs.n && s_wbeg[j + 1] <= w) ++j;
+      s_w = w;
+      s_j = j;
+    }
+    __syncthreads();
+    const uint32_t w = s_w;
+    const int j = s_j;
+    __syncthreads();  // every thread has read s_w, s_j
+    if (w >= total) break;
+    const GridJob &jb = jobs.job[j];
+    const uint32_t ci = s_cbeg[j] + (w - s_wbeg[j]);
+    degrid_lane_chunk<NP, WT>(jb.g, reinterpret_cast<const ItemF *>(jb.items), jb.chunks[ci],
+                              jb.b0, jb.nb, reinterpret_cast<const float2 *>(jb.grid),
+                              reinterpret_cast<float2 *>(jb.vis), jb.npv, jb.wgt, pm, jb.rp,
+                              stage, skv);
+  }
+}
+
 size_t degrid_lane_smem_bytes(const gb_plan *p) {
   const int SW = p->g.T + p->g.W - 1;
   return (size_t)2 * SW * lane_row(p->g.NP, SW) * sizeof(float2) +
@@ -576,88 +655,236 @@ static int setup_degrid_lane(gb_plan *p) {
   return GB_OK;
 }
 
+// The predict driver in steps (gb_batch.cu interleaves them across plans):
+// begin (corrected image), then per w-plane batch bi: transform (screens +
+// 2-D transform into the batch buffer), degrid.
 template <typename R, int NP>
-static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *wgt,
-                         const PolMat &pm, int npv, void *vis, cudaStream_t s) {
+static int pred_begin_impl(gb_plan *p, const void *dirty, int layout, cudaStream_t s) {
+  const Geom &g = p->g;
+  R *img = reinterpret_cast<R *>(p->ws + p->off_temp + p->c_img);
+  uint32_t *counters = p->at<uint32_t>(p->off_counters) + p->nbatches;
+  GB_CUDA(cudaMemsetAsync(counters, 0, 4 * (size_t)p->nbatches, s));
+  dim3 fb((g.nx + 31) / 32, (g.ny + 31) / 32, NP);
+  const double npix = (double)g.nx * g.ny;
+  ProfScope ps(kProfPrepImage, s, 3.0 * sizeof(R) * NP * npix);
+  k_prep_image<R><<<fb, dim3(32, 8), 0, s>>>(g, reinterpret_cast<const R *>(dirty), layout,
+                                             p->at<R>(p->off_corr), img);
+  GB_LAUNCH_CHECK("k_prep_image");
+  return GB_OK;
+}
+
+template <typename R, int NP>
+static int pred_transform_impl(gb_plan *p, int bi, cudaStream_t s) {
   using C = typename Traits<R>::C;
-  using Item = typename Traits<R>::Item;
   const Geom &g = p->g;
   char *tmp = p->ws + p->off_temp;
   C *grid = reinterpret_cast<C *>(tmp + p->c_grid);
   R *img = reinterpret_cast<R *>(tmp + p->c_img);
+  const int b0 = bi * g.B, nb = std::min(g.B, g.nplanes - b0);
+  const int64_t plane = (int64_t)g.ngx * g.ngy;
+  const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
+  const double npix = (double)g.nx * g.ny;
+  bool cols = false;
+  if constexpr (std::is_same<R, float>::value) {
+    if (p->col_fft) {  // screen + columns now, rows below
+      const int rc = run_cols_predict(p, img, b0, nb, grid, s);
+      if (rc) return rc;
+      cols = true;
+    }
+  }
+  if (!cols) {
+    const unsigned cell_blocks = (unsigned)std::min<int64_t>((plane + kThreads - 1) / kThreads,
+                                                             (int64_t)p->num_sms * 32);
+    ProfScope ps(kProfScreenPad, s, gbytes + sizeof(R) * NP * npix);
+    k_screen_pad<R, NP><<<cell_blocks, kThreads, 0, s>>>(g, img, p->at<double>(p->off_tprime),
+                                                         b0, nb, grid);
+    GB_LAUNCH_CHECK("k_screen_pad");
+  }
+  if (p->row_fft) {
+    // image half in, row out
+    ProfScope ps(kProfRowsFwd, s, 1.5 * p->used_rows(b0, nb) * gbytes);
+    return run_rows(p, grid, b0, nb, -1, s);
+  }
+  ProfScope ps(kProfFftFwd, s, 2.0 * gbytes);
+  return run_fft(p, nb, grid, CUFFT_FORWARD, s);
+}
+
+// Algorithmic bytes and updates of degridding batch bi (profiling): items
+// read, their vis written once; the grid cells they reach read once (the
+// cells of the (plane, tile) pairs reached, else the rows).
+template <typename R, int NP>
+static void degrid_counts(const gb_plan *p, int bi, int npv, bool wgt, double *bytes,
+                          double *updates) {
+  using C = typename Traits<R>::C;
+  using Item = typename Traits<R>::Item;
+  const Geom &g = p->g;
+  const int b0 = bi * g.B, nb = std::min(g.B, g.nplanes - b0);
+  const double gbytes = (double)sizeof(C) * nb * NP * (double)g.ngx * g.ngy;
+  const double cells = p->touched_cells(b0, nb);
+  const double gread = cells > 0.0 ? cells * NP * sizeof(C) : p->used_rows(b0, nb) * gbytes;
+  *bytes = (double)p->batch_items(b0, nb) *
+               (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) + gread;
+  *updates = p->item_planes(b0, nb) * g.W * g.W * NP;
+}
+
+template <typename R, int NP>
+static int pred_degrid_impl(gb_plan *p, int bi, const void *wgt, const PolMat &pm, int npv,
+                            void *vis, cudaStream_t s) {
+  using C = typename Traits<R>::C;
+  using Item = typename Traits<R>::Item;
+  const Geom &g = p->g;
+  C *grid = reinterpret_cast<C *>(p->ws + p->off_temp + p->c_grid);
   uint32_t *counters = p->at<uint32_t>(p->off_counters) + p->nbatches;
   const Item *items = p->at<Item>(p->off_items);
   const Chunk *chunks = p->at<Chunk>(p->off_chunks);
   const uint32_t *chunk_off = p->at<uint32_t>(p->off_chunk_off);
-  const R *corr = p->at<R>(p->off_corr);
-  GB_CUDA(cudaMemsetAsync(counters, 0, 4 * (size_t)p->nbatches, s));
-  dim3 fb((g.nx + 31) / 32, (g.ny + 31) / 32, NP);
-  const double npix = (double)g.nx * g.ny;
-  {
-    ProfScope ps(kProfPrepImage, s, 3.0 * sizeof(R) * NP * npix);
-    k_prep_image<R><<<fb, dim3(32, 8), 0, s>>>(g, reinterpret_cast<const R *>(dirty), layout,
-                                               corr, img);
-    GB_LAUNCH_CHECK("k_prep_image");
-  }
-  const int64_t plane = (int64_t)g.ngx * g.ngy;
-  const unsigned cell_blocks = (unsigned)std::min<int64_t>((plane + kThreads - 1) / kThreads,
-                                                           (int64_t)p->num_sms * 32);
-  const size_t smem = tile_smem_bytes(p);
+  const int b0 = bi * g.B, nb = std::min(g.B, g.nplanes - b0);
   const RowPerm rperm = row_perm(p);
   C *vis_c = reinterpret_cast<C *>(vis);
-  for (int bi = 0; bi < p->nbatches; ++bi) {
-    const int b0 = bi * g.B;
-    const int nb = std::min(g.B, g.nplanes - b0);
-    const double gbytes = (double)sizeof(C) * nb * NP * (double)plane;
-    bool cols = false;
-    if constexpr (std::is_same<R, float>::value) {
-      if (p->col_fft) {  // screen + columns now, rows below
-        const int rc = run_cols_predict(p, img, b0, nb, grid, s);
-        if (rc) return rc;
-        cols = true;
-      }
-    }
-    if (!cols) {
-      ProfScope ps(kProfScreenPad, s, gbytes + sizeof(R) * NP * npix);
-      k_screen_pad<R, NP><<<cell_blocks, kThreads, 0, s>>>(g, img, p->at<double>(p->off_tprime),
-                                                           b0, nb, grid);
-      GB_LAUNCH_CHECK("k_screen_pad");
-    }
-    int rc;
-    if (p->row_fft) {
-      ProfScope ps(kProfRowsFwd, s, 1.5 * p->used_rows(b0, nb) * gbytes);  // image half in, row out
-      rc = run_rows(p, grid, b0, nb, -1, s);
-    } else {
-      ProfScope ps(kProfFftFwd, s, 2.0 * gbytes);
-      rc = run_fft(p, nb, grid, CUFFT_FORWARD, s);
-    }
-    if (rc) return rc;
-    {
-      const double nbi = (double)p->batch_items(b0, nb);
-      // items read, their vis written once; the grid cells they reach read
-      // once (the cells of the (plane, tile) pairs reached, else the rows)
-      const double cells = p->touched_cells(b0, nb);
-      const double gread = cells > 0.0 ? cells * NP * sizeof(C) : p->used_rows(b0, nb) * gbytes;
-      ProfScope ps(kProfDegrid, s,
-                   nbi * (sizeof(Item) + npv * sizeof(C) + (wgt ? npv * sizeof(R) : 0.0)) + gread,
-                   p->item_planes(b0, nb) * g.W * g.W * NP);
-      if constexpr (std::is_same<R, float>::value) {
-        launch_degrid_lane<NP>(p, (unsigned)p->degrid_blocks, degrid_lane_smem_bytes(p), s, items,
-                               chunks, chunk_off, b0, nb, grid, vis_c, npv,
-                               reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
-      } else {
-        if (group_lanes(g.W) == 8)
-          k_degrid<R, NP, 8><<<p->degrid_blocks, kThreads, smem, s>>>(
-              g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv,
-              reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
-        else
-          k_degrid<R, NP, 16><<<p->degrid_blocks, kThreads, smem, s>>>(
-              g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv,
-              reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
-      }
-      GB_LAUNCH_CHECK("k_degrid");
-    }
+  double bytes = 0.0, updates = 0.0;
+  if (prof_on()) degrid_counts<R, NP>(p, bi, npv, wgt != nullptr, &bytes, &updates);
+  ProfScope ps(kProfDegrid, s, bytes, updates);
+  if constexpr (std::is_same<R, float>::value) {
+    launch_degrid_lane<NP>(p, (unsigned)p->degrid_blocks, degrid_lane_smem_bytes(p), s, items,
+                           chunks, chunk_off, b0, nb, grid, vis_c, npv,
+                           reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
+  } else {
+    const size_t smem = tile_smem_bytes(p);
+    if (group_lanes(g.W) == 8)
+      k_degrid<R, NP, 8><<<p->degrid_blocks, kThreads, smem, s>>>(
+          g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv, reinterpret_cast<const R *>(wgt),
+          pm, rperm, counters + bi);
+    else
+      k_degrid<R, NP, 16><<<p->degrid_blocks, kThreads, smem, s>>>(
+          g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv, reinterpret_cast<const R *>(wgt),
+          pm, rperm, counters + bi);
   }
+  GB_LAUNCH_CHECK("k_degrid");
+  return GB_OK;
+}
+
+template <typename R, int NP>
+static int dirty2ms_impl(gb_plan *p, const void *dirty, int layout, const void *wgt,
+                         const PolMat &pm, int npv, void *vis, cudaStream_t s) {
+  int rc = pred_begin_impl<R, NP>(p, dirty, layout, s);
+  for (int bi = 0; !rc && bi < p->nbatches; ++bi) {
+    rc = pred_transform_impl<R, NP>(p, bi, s);
+    if (!rc) rc = pred_degrid_impl<R, NP>(p, bi, wgt, pm, npv, vis, s);
+  }
+  return rc;
+}
+
+#define GB_PRED_DISPATCH(p, CALL)                    \
+  do {                                               \
+    if ((p)->precision == GB_FP64) {                 \
+      switch ((p)->g.NP) {                           \
+        case 1: { using R = double; constexpr int NP = 1; return CALL; } \
+        case 2: { using R = double; constexpr int NP = 2; return CALL; } \
+        default: { using R = double; constexpr int NP = 4; return CALL; } \
+      }                                              \
+    }                                                \
+    switch ((p)->g.NP) {                             \
+      case 1: { using R = float; constexpr int NP = 1; return CALL; } \
+      case 2: { using R = float; constexpr int NP = 2; return CALL; } \
+      default: { using R = float; constexpr int NP = 4; return CALL; } \
+    }                                                \
+  } while (0)
+
+int pred_begin(gb_plan *p, const void *dirty, int layout, cudaStream_t s) {
+  GB_PRED_DISPATCH(p, (pred_begin_impl<R, NP>(p, dirty, layout, s)));
+}
+int pred_transform(gb_plan *p, int bi, cudaStream_t s) {
+  GB_PRED_DISPATCH(p, (pred_transform_impl<R, NP>(p, bi, s)));
+}
+
+// Fill one job of a multi-plan degridding launch from a bound FP32 plan
+// whose batch bi has been transformed.
+int degrid_job(gb_plan *p, int bi, void *vis, int npv, GridJob &jb) {
+  if (p->precision != GB_FP32 || !p->bound || bi < 0 || bi >= p->nbatches) {
+    set_error("degrid_job: needs a bound FP32 plan and a batch index in range");
+    return GB_ERR_INVALID_ARG;
+  }
+  char *tmp = p->ws + p->off_temp;
+  jb.g = p->g;
+  jb.items = p->at<ItemF>(p->off_items);
+  jb.cvis = nullptr;
+  jb.chunks = p->at<Chunk>(p->off_chunks);
+  jb.chunk_off = p->at<uint32_t>(p->off_chunk_off);
+  jb.grid = tmp + p->c_grid;
+  jb.b0 = bi * p->g.B;
+  jb.nb = std::min(p->g.B, p->g.nplanes - jb.b0);
+  jb.vis = vis;
+  jb.npv = npv;
+  jb.pad = 0;
+  jb.wgt = nullptr;
+  jb.rp = row_perm(p);
+  return GB_OK;
+}
+
+void degrid_job_counts(const gb_plan *p, int bi, int npv, double *bytes, double *updates) {
+  *bytes = 0.0;
+  *updates = 0.0;
+  if (!prof_on()) return;
+  switch (p->g.NP) {
+    case 1: degrid_counts<float, 1>(p, bi, npv, false, bytes, updates); break;
+    case 2: degrid_counts<float, 2>(p, bi, npv, false, bytes, updates); break;
+    default: degrid_counts<float, 4>(p, bi, npv, false, bytes, updates); break;
+  }
+}
+
+// One launch over `jobs` (all of one NP and support W, unit weights, one pol
+// matrix); `counter` must be zero.
+int launch_degrid_jobs(const GridJobs &jobs, const PolMat &pm, int num_sms, uint32_t *counter,
+                       double bytes, double updates, cudaStream_t s) {
+  if (jobs.n < 1 || jobs.n > kMaxJobs) {
+    set_error("launch_degrid_jobs: %d jobs (1..%d)", jobs.n, kMaxJobs);
+    return GB_ERR_INVALID_ARG;
+  }
+  const int NP = jobs.job[0].g.NP, W = jobs.job[0].g.W;
+  int pstride = 0;
+  for (int j = 0; j < jobs.n; ++j) {
+    const Geom &g = jobs.job[j].g;
+    if (g.NP != NP || g.W != W) {
+      set_error("launch_degrid_jobs: jobs of one launch share NP and the support");
+      return GB_ERR_INVALID_ARG;
+    }
+    const int SW = g.T + W - 1;
+    pstride = std::max(pstride, SW * lane_row(NP, SW));
+  }
+  const size_t smem = (size_t)2 * pstride * sizeof(float2) + (size_t)W * kThreads * sizeof(float);
+  ProfScope ps(kProfDegrid, s, bytes, updates);
+#define GB_DJ(NPV, WV)                                                                        \
+  case WV: {                                                                                  \
+    auto k = k_degrid_lane_jobs<NPV, WV>;                                                     \
+    GB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));  \
+    int per_sm = 0;                                                                           \
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem));       \
+    if (per_sm < 1) {                                                                         \
+      set_error("k_degrid_lane_jobs cannot launch with %zu bytes of shared memory", smem);   \
+      return GB_ERR_INVALID_ARG;                                                              \
+    }                                                                                         \
+    k<<<per_sm * num_sms, kThreads, smem, s>>>(jobs, pm, counter);                           \
+    break;                                                                                    \
+  }
+#define GB_DJ_NP(NPV)                                                                  \
+  switch (W) {                                                                         \
+    GB_DJ(NPV, 4) GB_DJ(NPV, 5) GB_DJ(NPV, 6) GB_DJ(NPV, 7) GB_DJ(NPV, 8) GB_DJ(NPV, 9)  \
+    GB_DJ(NPV, 10) GB_DJ(NPV, 11) GB_DJ(NPV, 12) GB_DJ(NPV, 13) GB_DJ(NPV, 14)          \
+    GB_DJ(NPV, 15) GB_DJ(NPV, 16)                                                        \
+    default:                                                                             \
+      set_error("support %d outside 4..16", W);                                          \
+      return GB_ERR_INVALID_ARG;                                                         \
+  }
+  if (NP == 1) {
+    GB_DJ_NP(1)
+  } else if (NP == 2) {
+    GB_DJ_NP(2)
+  } else {
+    GB_DJ_NP(4)
+  }
+#undef GB_DJ_NP
+#undef GB_DJ
+  GB_LAUNCH_CHECK("k_degrid_lane_jobs");
   return GB_OK;
 }
 
