@@ -951,10 +951,17 @@ def bench_lists(args):
 
     res = {}
     for streams in (1, 4, 8):
+        # the list as one device program on `streams` workspace slots
         dt = timed(lambda: wf.invert_list_rsexecute_workflow(blocks, models, "ng",
                                                              streams=streams, **kw))
         res["invert_list_streams_%d" % streams] = {"s": round(dt, 3),
                                                    "value": round(nvis / dt / 1e6, 2)}
+    dt = timed(lambda: wf.invert_list_rsexecute_workflow(blocks, models, "ng", streams=4,
+                                                         program=False, **kw))
+    res["invert_list_thread_map_streams_4"] = {"s": round(dt, 3),
+                                               "value": round(nvis / dt / 1e6, 2)}
+    dt = timed(lambda: wf.predict_list_rsexecute_workflow(blocks, models, "ng", streams=8, **kw))
+    res["predict_list_streams_8"] = {"s": round(dt, 3), "value": round(nvis / dt / 1e6, 2)}
     dt_res = timed(lambda: wf.residual_list_rsexecute_workflow(blocks, models, "ng", streams=4,
                                                                **kw))
 
@@ -987,7 +994,7 @@ def bench_lists(args):
         "wall_s": round(wall, 3), "kernel_s": round(busy, 3),
         "top": {k: {"ms": round(v["ms"], 1), "launches": v["launches"]} for k, v in top}}
     clear_plan_cache(release_memory=True)
-    best = max((v["value"], k) for k, v in res.items() if k.startswith("invert_list"))
+    best = max((v["value"], k) for k, v in res.items() if k.startswith("invert_list_streams"))
     # CPU baseline: the oracle's C gridder (ms2dirty, FP64, all cores) over
     # the first snapshots until ~10 s of work
     from oracle import cgridder

@@ -346,6 +346,40 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
                  const void *const *vis, void *const *dirty, const void *const *model,
                  void *const *pred, int32_t layout);
 
+/* The same program with every solve's full argument list: the invert and
+ * predict arguments of gb_plan_ms2dirty / gb_plan_dirty2ms per plan, so the
+ * list workflows (invert_list / predict_list over blocks with flags,
+ * imaging weights and polarisation frames, imaging_rsexecute.py:72-157)
+ * run as one device program.  Per round, the gridding of every slot's
+ * current plan runs in one persistent launch per (polarisations, lane
+ * width) and the degridding in one per (polarisations, support, output
+ * polarisation matrix), each fed from a device work queue; bucket sorts,
+ * transforms and screens run on the slot streams.  nslots <= 16; streams[0]
+ * carries the launches shared by all slots and ends after all the work.
+ * Asynchronous; capturable in a CUDA graph. */
+typedef struct {
+  /* invert (vis or psf non-zero: grid; else skipped) */
+  const void *vis;           /* [nrows][nchan][npol_vis] complex, or NULL with psf   */
+  int32_t npol_vis;
+  int32_t psf;
+  const void *wgt;           /* like vis, real; NULL = 1                              */
+  const void *flags;         /* like vis, flags_type; NULL = none                     */
+  int32_t flags_type;
+  int32_t pad0;
+  const double *polmat_in;   /* host, npol x npol_vis complex; NULL = identity        */
+  void *dirty;               /* [npol] images in `layout`                             */
+  double *sumwt;             /* [npol] or NULL                                        */
+  /* predict (model non-NULL: degrid; else skipped) */
+  const void *model;         /* [npol] images in `layout`                             */
+  const double *polmat_out;  /* host, npol_out x npol complex; NULL = identity        */
+  int32_t npol_out;
+  int32_t pad1;
+  void *pred;                /* [nrows][nchan][npol_out] complex (written)            */
+} gb_batch_item;
+int gb_batch_run_items(gb_plan *const *plans, const gb_batch_item *items, int32_t nplans,
+                       void *const *workspaces, const size_t *workspace_bytes,
+                       void *const *streams, int32_t nslots, int32_t layout);
+
 /* Tangent-plane phase rotation of visibilities in place, RASCIL's
  * phaserotate_visibility(tangent=True) (visibility/base.py:296-357) with
  * the phasor of calculate_blockvisibility_phasor (:1248-1264):

@@ -88,6 +88,27 @@ class PlanInfo(_c.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class BatchItem(_c.Structure):
+    """gb_batch_item: one solve's arguments in gb_batch_run_items."""
+    _fields_ = [
+        ("vis", _vp),
+        ("npol_vis", _c.c_int32),
+        ("psf", _c.c_int32),
+        ("wgt", _vp),
+        ("flags", _vp),
+        ("flags_type", _c.c_int32),
+        ("pad0", _c.c_int32),
+        ("polmat_in", _dp),
+        ("dirty", _vp),
+        ("sumwt", _vp),
+        ("model", _vp),
+        ("polmat_out", _dp),
+        ("npol_out", _c.c_int32),
+        ("pad1", _c.c_int32),
+        ("pred", _vp),
+    ]
+
+
 SIGNATURES = {
     "gb_plan_geometry": (_c.c_int, [_c.POINTER(PlanParams), _c.c_double, _c.c_double,
                                     _c.POINTER(PlanInfo)]),
@@ -103,6 +124,8 @@ SIGNATURES = {
     "gb_plan_device_status": (_c.c_int, [_vp, _vp, _c.POINTER(_c.c_int32)]),
     "gb_batch_run": (_c.c_int, [_vp, _c.c_int32, _vp, _vp, _vp, _c.c_int32, _vp, _vp, _vp,
                                 _vp, _c.c_int32]),
+    "gb_batch_run_items": (_c.c_int, [_vp, _c.POINTER(BatchItem), _c.c_int32, _vp, _vp, _vp,
+                                      _c.c_int32, _c.c_int32]),
     "gb_phase_rotate": (_c.c_int, [_vp, _vp, _c.c_int64, _c.c_int32, _c.c_int32, _vp,
                                    _c.c_int32, _c.c_double, _c.c_double, _c.c_double,
                                    _c.c_int32, _vp]),

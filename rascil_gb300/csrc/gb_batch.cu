@@ -50,40 +50,73 @@ struct Slot {
   bool grid_job = false, degrid_job = false;
 };
 
-PolMat identity_pm(int np) {
-  PolMat pm;
-  memset(&pm, 0, sizeof(pm));
-  pm.nout = pm.nin = np;
-  pm.identity = 1;
-  return pm;
+struct Args {  // one solve's arguments, validated, matrices built
+  gb_batch_item it;
+  PolMat pm_in, pm_out;
+  bool inv, pred;
+};
+
+bool same_pm(const PolMat &a, const PolMat &b) {
+  if (a.identity && b.identity) return a.nout == b.nout;
+  return a.identity == b.identity && a.nout == b.nout && a.nin == b.nin &&
+         memcmp(a.re, b.re, sizeof(a.re)) == 0 && memcmp(a.im, b.im, sizeof(a.im)) == 0;
 }
 
-}  // namespace
-
-extern "C" {
-
-int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
-                 const size_t *workspace_bytes, void *const *streams, int32_t nslots,
-                 const void *const *vis, void *const *dirty, const void *const *model,
-                 void *const *pred, int32_t layout) {
-  if (nplans < 0 || (nplans > 0 && (!plans || !workspaces || !workspace_bytes || !streams)) ||
+int run_items(gb_plan *const *plans, const gb_batch_item *items, int32_t nplans,
+              void *const *workspaces, const size_t *workspace_bytes, void *const *streams,
+              int32_t nslots, int32_t layout) {
+  if (nplans < 0 || (nplans > 0 && (!plans || !items || !workspaces || !workspace_bytes ||
+                                    !streams)) ||
       nslots < 1 || nslots > kMaxJobs) {
     set_error("gb_batch_run: NULL array, or nslots outside 1..%d", kMaxJobs);
     return GB_ERR_INVALID_ARG;
   }
+  if (layout != GB_LAYOUT_XY && layout != GB_LAYOUT_YX) {
+    set_error("gb_batch_run: unknown layout %d", layout);
+    return GB_ERR_INVALID_ARG;
+  }
+  std::vector<Args> args(nplans);
   for (int32_t i = 0; i < nplans; ++i) {
     gb_plan *p = plans[i];
+    Args &a = args[i];
+    a.it = items[i];
     if (!p) {
       set_error("gb_batch_run: plan %d is NULL", (int)i);
       return GB_ERR_INVALID_ARG;
     }
-    if (vis && vis[i] && (!dirty || !dirty[i])) {
-      set_error("gb_batch_run: plan %d has visibilities but no dirty image", (int)i);
-      return GB_ERR_INVALID_ARG;
+    a.inv = a.it.vis || a.it.psf;
+    a.pred = a.it.model != nullptr;
+    const int np = p->g.NP;
+    if (a.inv) {
+      if (!a.it.dirty) {
+        set_error("gb_batch_run: plan %d has visibilities but no dirty image", (int)i);
+        return GB_ERR_INVALID_ARG;
+      }
+      if (a.it.npol_vis < np || a.it.npol_vis > 4) {
+        set_error("gb_batch_run: plan %d: npol_vis %d outside [npol=%d, 4]", (int)i,
+                  a.it.npol_vis, np);
+        return GB_ERR_INVALID_ARG;
+      }
+      if (!a.it.flags) a.it.flags_type = GB_FLAGS_NONE;
+      if (a.it.flags && a.it.flags_type != GB_FLAGS_U8 && a.it.flags_type != GB_FLAGS_I64) {
+        set_error("gb_batch_run: plan %d: flags_type %d unknown", (int)i, a.it.flags_type);
+        return GB_ERR_INVALID_ARG;
+      }
+      const int rc = make_polmat(a.it.polmat_in, np, a.it.npol_vis, a.pm_in);
+      if (rc) return rc;
     }
-    if (model && model[i] && (!pred || !pred[i])) {
-      set_error("gb_batch_run: plan %d has a model but no output visibilities", (int)i);
-      return GB_ERR_INVALID_ARG;
+    if (a.pred) {
+      if (!a.it.pred) {
+        set_error("gb_batch_run: plan %d has a model but no output visibilities", (int)i);
+        return GB_ERR_INVALID_ARG;
+      }
+      if (a.it.npol_out < np || a.it.npol_out > 4) {
+        set_error("gb_batch_run: plan %d: npol_out %d outside [npol=%d, 4]", (int)i,
+                  a.it.npol_out, np);
+        return GB_ERR_INVALID_ARG;
+      }
+      const int rc = make_polmat(a.it.polmat_out, a.it.npol_out, np, a.pm_out);
+      if (rc) return rc;
     }
     if (workspace_bytes[i % nslots] < p->ws_bytes) {
       set_error("gb_batch_run: workspace %d holds %zu bytes, plan %d needs %zu", (int)(i % nslots),
@@ -103,19 +136,16 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
   }
   cudaEvent_t ev_main = nullptr;
   int rc = GB_OK;
-  auto fail = [&](int r) {
-    rc = r;
-    return r;
-  };
-#define GB_TRY(call)                 \
-  do {                               \
-    const int r__ = (call);          \
-    if (r__) {                       \
-      fail(r__);                     \
-      goto done;                     \
-    }                                \
+#define GB_TRY(call)      \
+  do {                    \
+    const int r__ = (call); \
+    if (r__) {            \
+      rc = r__;           \
+      goto done;          \
+    }                     \
   } while (0)
-#define GB_TRYC(call) GB_TRY(((call) == cudaSuccess) ? GB_OK : cuda_fail(cudaGetLastError(), #call))
+#define GB_TRYC(call) \
+  GB_TRY(((call) == cudaSuccess) ? GB_OK : cuda_fail(cudaGetLastError(), #call))
   GB_TRYC(cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming));
   for (auto &sl : slots) GB_TRYC(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
   for (;;) {
@@ -138,25 +168,27 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
         }
         const int i = sl.cur;
         gb_plan *p = plans[i];
-        const PolMat pm = identity_pm(p->g.NP);
+        const Args &a = args[i];
         if (sl.phase == kBind) {
           GB_TRY(gb_plan_bind(p, workspaces[k], workspace_bytes[k], sl.s));
           sl.bi = 0;
           if (p->precision == GB_FP64) {  // the FP64 form: whole calls per plan
-            if (vis && vis[i])
-              GB_TRY(run_ms2dirty(p, vis[i], p->g.NP, nullptr, nullptr, GB_FLAGS_NONE, pm, 0,
-                                  dirty[i], layout, nullptr, sl.s));
-            if (model && model[i])
-              GB_TRY(run_dirty2ms(p, model[i], layout, nullptr, pm, p->g.NP, pred[i], sl.s));
+            if (a.inv)
+              GB_TRY(run_ms2dirty(p, a.it.vis, a.it.npol_vis, a.it.wgt, a.it.flags,
+                                  a.it.flags_type, a.pm_in, a.it.psf, a.it.dirty, layout,
+                                  a.it.sumwt, sl.s));
+            if (a.pred)
+              GB_TRY(run_dirty2ms(p, a.it.model, layout, nullptr, a.pm_out, a.it.npol_out,
+                                  a.it.pred, sl.s));
             sl.phase = kDone;
             continue;
           }
-          if (vis && vis[i]) {
-            GB_TRY(inv_begin(p, vis[i], p->g.NP, nullptr, nullptr, GB_FLAGS_NONE, pm, 0, nullptr,
-                             sl.s));
+          if (a.inv) {
+            GB_TRY(inv_begin(p, a.it.vis, a.it.npol_vis, a.it.wgt, a.it.flags, a.it.flags_type,
+                             a.pm_in, a.it.psf, a.it.sumwt, sl.s));
             sl.phase = kInvert;
-          } else if (model && model[i]) {
-            GB_TRY(pred_begin(p, model[i], layout, sl.s));
+          } else if (a.pred) {
+            GB_TRY(pred_begin(p, a.it.model, layout, sl.s));
             sl.phase = kPredict;
           } else {
             sl.phase = kDone;
@@ -184,7 +216,8 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
       for (int k0 = 0; k0 < nslots; ++k0) {
         const bool want0 = pass == 0 ? slots[k0].grid_job : slots[k0].degrid_job;
         if (!want0 || taken[k0]) continue;
-        gb_plan *p0 = plans[slots[k0].cur];
+        const int i0 = slots[k0].cur;
+        gb_plan *p0 = plans[i0];
         GridJobs jobs;
         jobs.n = 0;
         double bytes = 0.0, updates = 0.0;
@@ -193,9 +226,10 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
           const bool want = pass == 0 ? sl.grid_job : sl.degrid_job;
           if (!want || taken[k]) continue;
           gb_plan *p = plans[sl.cur];
-          const bool same = p->g.NP == p0->g.NP &&
-                            (pass == 0 ? group_lanes(p->g.W) == group_lanes(p0->g.W)
-                                       : p->g.W == p0->g.W);
+          const bool same =
+              p->g.NP == p0->g.NP &&
+              (pass == 0 ? group_lanes(p->g.W) == group_lanes(p0->g.W)
+                         : p->g.W == p0->g.W && same_pm(args[sl.cur].pm_out, args[i0].pm_out));
           if (!same) continue;
           taken[k] = true;
           double b = 0.0, u = 0.0;
@@ -203,8 +237,9 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
             GB_TRY(grid_job(p, sl.bi, jobs.job[jobs.n]));
             grid_job_counts(p, sl.bi, &b, &u);
           } else {
-            GB_TRY(degrid_job(p, sl.bi, pred[sl.cur], p->g.NP, jobs.job[jobs.n]));
-            degrid_job_counts(p, sl.bi, p->g.NP, &b, &u);
+            const Args &a = args[sl.cur];
+            GB_TRY(degrid_job(p, sl.bi, a.it.pred, a.it.npol_out, jobs.job[jobs.n]));
+            degrid_job_counts(p, sl.bi, a.it.npol_out, &b, &u);
           }
           bytes += b;
           updates += u;
@@ -216,8 +251,7 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
         if (pass == 0)
           GB_TRY(launch_grid_jobs(jobs, sms, counter, bytes, updates, main));
         else
-          GB_TRY(launch_degrid_jobs(jobs, identity_pm(p0->g.NP), sms, counter, bytes, updates,
-                                    main));
+          GB_TRY(launch_degrid_jobs(jobs, args[i0].pm_out, sms, counter, bytes, updates, main));
       }
     }
     // fork: the invert jobs' transforms; advance every slot
@@ -227,14 +261,15 @@ int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
       if (!sl.grid_job && !sl.degrid_job) continue;
       const int i = sl.cur;
       gb_plan *p = plans[i];
+      const Args &a = args[i];
       if (sl.grid_job) {
         GB_TRYC(cudaStreamWaitEvent(sl.s, ev_main, 0));
         GB_TRY(inv_transform(p, sl.bi, sl.s));
         if (++sl.bi == p->nbatches) {
-          GB_TRY(inv_end(p, dirty[i], layout, sl.s));
+          GB_TRY(inv_end(p, a.it.dirty, layout, sl.s));
           sl.bi = 0;
-          if (model && model[i]) {
-            GB_TRY(pred_begin(p, model[i], layout, sl.s));
+          if (a.pred) {
+            GB_TRY(pred_begin(p, a.it.model, layout, sl.s));
             sl.phase = kPredict;
           } else {
             sl.phase = kDone;
@@ -257,6 +292,44 @@ done:
 #undef GB_TRYC
 #undef GB_TRY
   return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gb_batch_run_items(gb_plan *const *plans, const gb_batch_item *items, int32_t nplans,
+                       void *const *workspaces, const size_t *workspace_bytes,
+                       void *const *streams, int32_t nslots, int32_t layout) {
+  return run_items(plans, items, nplans, workspaces, workspace_bytes, streams, nslots, layout);
+}
+
+int gb_batch_run(gb_plan *const *plans, int32_t nplans, void *const *workspaces,
+                 const size_t *workspace_bytes, void *const *streams, int32_t nslots,
+                 const void *const *vis, void *const *dirty, const void *const *model,
+                 void *const *pred, int32_t layout) {
+  if (nplans < 0 || (nplans > 0 && !plans)) {
+    set_error("gb_batch_run: NULL plans");
+    return GB_ERR_INVALID_ARG;
+  }
+  std::vector<gb_batch_item> items(nplans > 0 ? nplans : 0);
+  for (int32_t i = 0; i < nplans; ++i) {
+    gb_batch_item &it = items[i];
+    memset(&it, 0, sizeof(it));
+    const int np = plans[i] ? plans[i]->g.NP : 1;
+    it.vis = vis ? vis[i] : nullptr;
+    it.npol_vis = np;
+    it.dirty = dirty ? dirty[i] : nullptr;
+    it.model = model ? model[i] : nullptr;
+    it.npol_out = np;
+    it.pred = pred ? pred[i] : nullptr;
+    if (it.vis && !it.dirty) {
+      set_error("gb_batch_run: plan %d has visibilities but no dirty image", (int)i);
+      return GB_ERR_INVALID_ARG;
+    }
+  }
+  return run_items(plans, items.data(), nplans, workspaces, workspace_bytes, streams, nslots,
+                   layout);
 }
 
 }  // extern "C"

@@ -7,7 +7,8 @@
 
 using namespace gb;
 
-static int make_polmat(const double *host, int nout, int nin, PolMat &pm) {
+namespace gb {
+int make_polmat(const double *host, int nout, int nin, PolMat &pm) {
   memset(&pm, 0, sizeof(pm));
   pm.nout = nout;
   pm.nin = nin;
@@ -31,6 +32,7 @@ static int make_polmat(const double *host, int nout, int nin, PolMat &pm) {
   }
   return GB_OK;
 }
+}  // namespace gb
 
 extern "C" {
 

@@ -140,6 +140,10 @@ int inv_end(gb_plan *p, void *dirty, int layout, cudaStream_t s);
 int pred_begin(gb_plan *p, const void *dirty, int layout, cudaStream_t s);
 int pred_transform(gb_plan *p, int bi, cudaStream_t s);
 
+// Polarisation matrix from a host array of nout x nin complex (re, im
+// interleaved; NULL = identity, which needs nout == nin).
+int make_polmat(const double *host, int nout, int nin, PolMat &pm);
+
 // One plan's batch of w-planes in a multi-plan gridding or degridding launch
 // (FP32 form), passed to the kernel by value.
 constexpr int kMaxJobs = 16;

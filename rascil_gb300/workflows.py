@@ -6,11 +6,19 @@ per block through Dask and then summing the results
 (``rascil/workflows/rsexecute/imaging/imaging_rsexecute.py:72-181,844-931``,
 ``rascil/processing_components/imaging/imaging_helpers.py:17-72``).  Here
 the same functions, with the same arguments, results and side effects, run
-the blocks concurrently on one GPU:
+the blocks on one GPU:
 
-* a pool of worker threads, each with its own CUDA stream, takes the blocks
-  in order; one block's transfers, bucket sort, gridding and transforms
-  overlap another's (ctypes and torch release the GIL while they wait);
+* ``invert_list`` / ``predict_list`` over blocks whose visibility channels
+  all map to one image channel (MFS images, or one channel per block) run
+  as ONE device program (``gb_batch_run_items``): every block's arrays are
+  uploaded, one plan per block, then rounds over workspace slots in which
+  the gridding (or degridding) of every slot's block runs in one persistent
+  launch fed from a device work queue, with each block's transforms on its
+  slot's stream;
+* other lists (several image channels per block) run on a pool of worker
+  threads, each with its own CUDA stream; one block's transfers, bucket
+  sort, gridding and transforms overlap another's (ctypes and torch release
+  the GIL while they wait);
 * the residual workflow runs each block's predict, subtraction and invert
   on the device in one pass (``residual_ng``), so the model visibilities
   never travel to the host and back;
@@ -114,15 +122,228 @@ def _map_blocks(func, items, nstreams):
         return list(pool.map(run, items))
 
 
+# ---------------------------------------------------------------------------
+# the list as one device program (gb_batch_run_items)
+
+def _single_group(bvis, model):
+    """The image channel all of the block's visibility channels map to (the
+    block then needs one plan, as the device program takes), else None."""
+    from .imaging.ng import _vis_to_im
+    freq = numpy.asarray(bvis.frequency.data, dtype=numpy.float64)
+    nchan = model["pixels"].data.shape[0]
+    if nchan == 1:
+        return 0
+    v2i = numpy.unique(_vis_to_im(model, freq))
+    return int(v2i[0]) if len(v2i) == 1 else None
+
+
+def _batchable(vis_list, models, context):
+    if context not in ("ng", "gb", "2d") or not torch.cuda.is_available() or len(vis_list) < 2:
+        return False
+    for bvis, model in zip(vis_list, models):
+        if bvis is None or model is None:
+            return False
+        nrows, nbl, vnchan, _ = bvis.vis.shape
+        if nrows * nbl == 0 or vnchan == 0 or _single_group(bvis, model) is None:
+            return False
+        if not numpy.isfinite(numpy.asarray(bvis.uvw.data)).all():
+            return False
+    return True
+
+
+def _run_program(plans, items, nslots, device):
+    """gb_batch_run_items over the plans on nslots workspace slots and
+    streams, ordered after (and before) the current stream's work."""
+    import ctypes
+
+    from . import _lib
+    n = len(plans)
+    nslots = max(1, min(nslots, n, 16))
+    need = [256] * nslots
+    for i, p in enumerate(plans):
+        need[i % nslots] = max(need[i % nslots], p.workspace_bytes)
+    workspaces = [torch.empty(b, dtype=torch.uint8, device=device) for b in need]
+    origin = torch.cuda.current_stream(device)
+    streams = [origin] + [torch.cuda.Stream(device=device) for _ in range(nslots - 1)]
+    for st in streams[1:]:
+        st.wait_stream(origin)
+    ptrs = (ctypes.c_void_p * n)(*[p._handle.value for p in plans])
+    arr = (_lib.BatchItem * n)(*items)
+    ws = (ctypes.c_void_p * nslots)(*[w.data_ptr() for w in workspaces])
+    wsb = (ctypes.c_size_t * nslots)(*[w.numel() for w in workspaces])
+    sts = (ctypes.c_void_p * nslots)(*[st.cuda_stream for st in streams])
+    with torch.cuda.device(device):
+        _lib.check(_lib.load().gb_batch_run_items(ptrs, arr, n, ws, wsb, sts, nslots,
+                                                  _lib.GB_LAYOUT_YX), "gb_batch_run_items")
+    for w in workspaces:  # the allocator must not recycle them under pending work
+        for st in streams:
+            w.record_stream(st)
+    for p, i in zip(plans, range(n)):
+        p.workspace = workspaces[i % nslots]
+
+
+def _polmat_ptr(m, keep):
+    import ctypes
+    if m is None:
+        return None
+    flat = numpy.ascontiguousarray(numpy.asarray(m, dtype=numpy.complex128).view(numpy.float64)
+                                   .ravel())
+    keep.append(flat)
+    return flat.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _invert_list_program(vis_list, models, dopsf, normalise, kwargs, nslots):
+    """invert_ng of every block (one plan each) as one device program."""
+    from . import _lib
+    from .imaging.base import fused_phase_shift
+    from .imaging.ng import _budget, _device_uvw, _to_device, _to_host, get_parameter
+    from .polarisation import conversion_matrix
+    from .wgridder import Plan
+    epsilon = get_parameter(kwargs, "epsilon", 1e-12)
+    do_wstacking = get_parameter(kwargs, "do_wstacking", True)
+    precision = get_parameter(kwargs, "precision", "fp64")
+    device = torch.device(get_parameter(kwargs, "device", "cuda"))
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    rdt = torch.float64 if precision == "fp64" else torch.float32
+    plans, items, outs, keep = [], [], [], []
+    try:
+        for bvis, model in zip(vis_list, models):
+            _, shift = fused_phase_shift(bvis, model)
+            freq = numpy.asarray(bvis.frequency.data, dtype=numpy.float64)
+            nrows, nbaselines, vnchan, vnpol = bvis.vis.shape
+            nchan, npol, ny, nx = model["pixels"].data.shape
+            R = nrows * nbaselines
+            pixsize = abs(numpy.radians(model.image_acc.wcs.wcs.cdelt[0]))
+            polmat = conversion_matrix(bvis.blockvisibility_acc.polarisation_frame,
+                                       model.image_acc.polarisation_frame)
+            pm = None if (npol == vnpol and numpy.array_equal(polmat, numpy.eye(vnpol))) \
+                else polmat
+            uvw = _device_uvw(bvis.uvw.data, device)
+            f = torch.from_numpy(freq.copy()).to(device)
+            vis = None if dopsf else _to_device(bvis["vis"].data.reshape(R, vnchan, vnpol), cdt,
+                                                device)
+            flags = _to_device(bvis["flags"].data.reshape(R, vnchan, vnpol), None, device)
+            if flags.dtype != torch.int64:
+                flags = (flags != 0).to(torch.uint8)
+            wgt = _to_device(bvis["imaging_weight"].data.reshape(R, vnchan, vnpol), rdt, device)
+            plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=npol,
+                        precision=precision, bind=False, phase_shift=shift,
+                        grid_budget_bytes=_budget(kwargs))
+            plans.append(plan)
+            dirty = torch.empty((npol, ny, nx), dtype=rdt, device=device)
+            sumwt = torch.empty(npol, dtype=torch.float64, device=device)
+            keep.append((uvw, f, vis, flags, wgt))
+            items.append(_lib.BatchItem(
+                vis=None if vis is None else vis.data_ptr(), npol_vis=vnpol,
+                psf=1 if dopsf else 0, wgt=wgt.data_ptr(), flags=flags.data_ptr(),
+                flags_type=_lib.GB_FLAGS_I64 if flags.dtype == torch.int64 else _lib.GB_FLAGS_U8,
+                polmat_in=_polmat_ptr(pm, keep), dirty=dirty.data_ptr(),
+                sumwt=sumwt.data_ptr(), model=None, polmat_out=None, npol_out=npol, pred=None))
+            outs.append((dirty, sumwt))
+        _run_program(plans, items, nslots, device)
+        results = []
+        for (dirty, sw), bvis, model in zip(outs, vis_list, models):
+            ichan = _single_group(bvis, model)
+            nchan, npol, ny, nx = model["pixels"].data.shape
+            acc = torch.zeros((nchan, npol, ny, nx), dtype=torch.float64, device=device)
+            acc[ichan] = dirty
+            sumwt = numpy.zeros([nchan, npol])
+            sumwt[ichan] = sw.cpu().numpy()
+            if normalise:  # normalise_sumwt (imaging/base.py:109-162), on the device
+                scale = numpy.where(sumwt > 0.0, 1.0 / numpy.where(sumwt > 0.0, sumwt, 1.0), 0.0)
+                acc *= torch.from_numpy(scale).to(device)[:, :, None, None]
+            pdt = _torch_dtype(model["pixels"].data.dtype)
+            im = model.copy(deep=True,
+                            pixels=_to_host(acc if acc.dtype == pdt else acc.to(pdt), pdt))
+            results.append((im, sumwt))
+        return results
+    finally:
+        torch.cuda.current_stream(device).synchronize()
+        for p in plans:
+            p.close()
+
+
+def _predict_list_program(vis_list, models, kwargs, nslots):
+    """predict_ng of every block (one plan each) as one device program."""
+    from . import _lib
+    from .imaging.base import fused_phase_shift
+    from .imaging.ng import _budget, _device_uvw, _to_device, _to_host, get_parameter
+    from .polarisation import conversion_matrix
+    from .wgridder import Plan
+    epsilon = get_parameter(kwargs, "epsilon", 1e-12)
+    do_wstacking = get_parameter(kwargs, "do_wstacking", True)
+    precision = get_parameter(kwargs, "precision", "fp64")
+    device = torch.device(get_parameter(kwargs, "device", "cuda"))
+    cdt = torch.complex128 if precision == "fp64" else torch.complex64
+    rdt = torch.float64 if precision == "fp64" else torch.float32
+    plans, items, outs, keep = [], [], [], []
+    try:
+        for bvis, model in zip(vis_list, models):
+            rotates, shift = fused_phase_shift(bvis, model)
+            freq = numpy.asarray(bvis.frequency.data, dtype=numpy.float64)
+            nrows, nbaselines, vnchan, vnpol = bvis.vis.shape
+            m_nchan, m_npol, ny, nx = model["pixels"].data.shape
+            assert m_npol == vnpol
+            pixsize = abs(numpy.radians(model.image_acc.wcs.wcs.cdelt[0]))
+            polmat = conversion_matrix(model.image_acc.polarisation_frame,
+                                       bvis.blockvisibility_acc.polarisation_frame)
+            pm = None if numpy.array_equal(polmat, numpy.eye(vnpol)) else polmat
+            uvw = _device_uvw(bvis.uvw.data, device, nan_to_num=True)
+            f = torch.from_numpy(freq.copy()).to(device)
+            ichan = _single_group(bvis, model)
+            img = _to_device(model["pixels"].data[ichan], rdt, device)
+            plan = Plan(uvw, f, nx, ny, pixsize, pixsize, epsilon, do_wstacking, npol=m_npol,
+                        precision=precision, bind=False, phase_shift=shift,
+                        grid_budget_bytes=_budget(kwargs))
+            plans.append(plan)
+            out = torch.empty((nrows * nbaselines, vnchan, vnpol), dtype=cdt, device=device)
+            keep.append((uvw, f, img))
+            items.append(_lib.BatchItem(vis=None, npol_vis=m_npol, psf=0, wgt=None, flags=None,
+                                        flags_type=0, polmat_in=None, dirty=None, sumwt=None,
+                                        model=img.data_ptr(), polmat_out=_polmat_ptr(pm, keep),
+                                        npol_out=vnpol, pred=out.data_ptr()))
+            outs.append((out, rotates))
+        _run_program(plans, items, nslots, device)
+        results = []
+        for (out, rotates), bvis, model in zip(outs, vis_list, models):
+            vdt = bvis["vis"].data.dtype
+            nrows, nbaselines, vnchan, vnpol = bvis.vis.shape
+            o = out.reshape(nrows, nbaselines, vnchan, vnpol)
+            want = torch.complex128 if vdt == numpy.complex128 else torch.complex64
+            if o.dtype != want:
+                o = o.to(want)
+            result = _to_host(o, o.dtype)
+            if result.dtype != vdt:
+                result = result.astype(vdt)
+            newbvis = copy_visibility(bvis, vis=result)
+            if rotates:
+                newbvis.attrs["phasecentre"] = model.image_acc.phasecentre
+            results.append(newbvis)
+        return results
+    finally:
+        torch.cuda.current_stream(device).synchronize()
+        for p in plans:
+            p.close()
+
+
 def invert_list_rsexecute_workflow(vis_list, template_model_imagelist, context, dopsf=False,
                                    normalise=True, **kwargs):
     """One (image, sumwt) per block (``imaging_rsexecute.py:115-157``).
-    Extra keyword: ``streams`` (concurrent blocks, default 4)."""
+    Extra keywords: ``streams`` (workspace slots of the device program, or
+    concurrent blocks on worker threads, default 4), ``program`` (False:
+    always the worker-thread map)."""
     if not isinstance(template_model_imagelist, collections.abc.Iterable):
         template_model_imagelist = [template_model_imagelist]
     template_model_imagelist = list(template_model_imagelist)
     assert len(template_model_imagelist) == len(vis_list)
+    program = kwargs.pop("program", True)
     nstreams = _streams(kwargs)
+    if program and _batchable(vis_list, template_model_imagelist, context):
+        kw = dict(kwargs)
+        if context == "2d":
+            kw["do_wstacking"] = False
+        return _invert_list_program(vis_list, template_model_imagelist, dopsf, normalise, kw,
+                                    max(nstreams, 1))
 
     def one(i):
         return invert_blockvisibility(vis_list[i], template_model_imagelist[i], dopsf=dopsf,
@@ -148,10 +369,16 @@ def zero_list_rsexecute_workflow(vis_list, copy=True):
 def predict_list_rsexecute_workflow(vis_list, model_imagelist, context, **kwargs):
     """Predicted copies of the blocks (``:72-112``).  As in the reference,
     the input blocks' visibilities are zeroed in place first."""
+    program = kwargs.pop("program", True)
     nstreams = _streams(kwargs)
     vis_list = zero_list_rsexecute_workflow(vis_list, copy=False)
     model_imagelist = list(model_imagelist)
     assert len(model_imagelist) == len(vis_list)
+    if program and _batchable(vis_list, model_imagelist, context):
+        kw = dict(kwargs)
+        if context == "2d":
+            kw["do_wstacking"] = False
+        return _predict_list_program(vis_list, model_imagelist, kw, max(nstreams, 1))
 
     def one(i):
         return predict_blockvisibility(vis_list[i], model_imagelist[i], context=context,

@@ -97,7 +97,7 @@ def test_residual_list_matches_composed_workflow(precision, eps, tol, offset):
     """residual_list (fused) == invert_list(subtract_list(vis, predict_list(
     zero_list(vis), models))) run block by block."""
     from rascil_gb300 import simulation as sim
-    from rascil_gb300.data_models import SkyDirection
+    from rascil_gb300.data_models import SkyDirection, copy_visibility
     from rascil_gb300.workflows import (invert_list_rsexecute_workflow,
                                         predict_list_rsexecute_workflow,
                                         residual_list_rsexecute_workflow,
@@ -164,3 +164,43 @@ def test_sum_of_block_inverts_equals_invert_of_all_rows(precision, eps, tol):
     ref, sw_ref = invert_ng(whole, model, **kw)
     numpy.testing.assert_allclose(sw, sw_ref, rtol=1e-12)
     assert rel_rms(im["pixels"].data, ref["pixels"].data) < tol
+
+
+def test_list_program_matches_worker_thread_map():
+    """invert_list / predict_list as one device program (gb_batch_run_items:
+    per round, every slot's block gridded or degridded in one persistent
+    launch) give the worker-thread map's results, with linear -> IQUV
+    polarisation matrices, flags, imaging weights and an image centred away
+    from the phase centre (the rotation fused into each block's plan)."""
+    from rascil_gb300 import simulation as sim
+    from rascil_gb300.data_models import SkyDirection, copy_visibility
+    from rascil_gb300.workflows import (invert_list_rsexecute_workflow,
+                                        predict_list_rsexecute_workflow)
+    uvw, freq, pc, cfg = sim.observation("small-array", seed=0, ntimes=12, npixel=128)
+    cfg = dict(cfg, pol="linear", image_pol="stokesIQUV")
+    rng = numpy.random.default_rng(6)
+    blocks = []
+    for t0, n in ((0, 3), (3, 4), (7, 5)):
+        shape = (n, uvw.shape[1], len(freq), 4)
+        vis = (rng.normal(size=shape) + 1j * rng.normal(size=shape)).astype(numpy.complex64)
+        b = sim.make_blockvisibility(uvw[t0:t0 + n], freq, pc, cfg, vis=vis)
+        b["imaging_weight"].data[...] = rng.uniform(0.5, 1.5, shape)
+        b["flags"].data[...] = (rng.uniform(size=shape) < 0.05).astype(numpy.int64)
+        blocks.append(b)
+    off = SkyDirection(pc.ra.rad + 0.002, pc.dec.rad - 0.001)
+    models = [sim.model_image(cfg, ([], [], [], [], []), off, freq) for _ in blocks]
+    for m in models:
+        m["pixels"].data[0, :, 60:64, 70:72] = rng.uniform(0.5, 1.0, (4, 4, 2))
+    kw = dict(epsilon=1e-5, precision="fp32", streams=2)
+    a = invert_list_rsexecute_workflow(blocks, models, "ng", program=True, **kw)
+    b = invert_list_rsexecute_workflow(blocks, models, "ng", program=False, **kw)
+    for (ia, sa), (ib, sb) in zip(a, b):
+        numpy.testing.assert_allclose(sa, sb, rtol=1e-6)
+        assert rel_rms(ia["pixels"].data, ib["pixels"].data) < 1e-5
+    pa = predict_list_rsexecute_workflow([copy_visibility(x) for x in blocks], models, "ng",
+                                         program=True, **kw)
+    pb = predict_list_rsexecute_workflow([copy_visibility(x) for x in blocks], models, "ng",
+                                         program=False, **kw)
+    for va, vb in zip(pa, pb):
+        assert rel_rms(va["vis"].data, vb["vis"].data) < 1e-5
+        assert va.phasecentre.ra.rad == vb.phasecentre.ra.rad
