@@ -1106,13 +1106,23 @@ def bench_autograd(args):
     obs = apply_gains(v_true, gt, a1, a2).to(torch.complex64).contiguous()
     del v_true
     plan = Plan(fu, f, npix, npix, cell, cell, eps, True, npol=1, precision="fp32")
-    # steepest-descent step sizes: the image's Hessian peak is 2 nvis (unit
-    # weights, gains near 1); the gains' is 2 sum over an antenna's rows of |V|^2
-    lr_x = 0.5 / nvis
-    vis_pow = float(obs.abs().pow(2).mean())
-    lr_g = 0.25 / ((nants - 1) * nt * max(vis_pow, 1e-30))
+    # image step 1 / L: L = 2 lambda_max(A^H A) (power iteration through the
+    # plan's own predict and adjoint) with a margin for gains near 1
+    with torch.no_grad():
+        xp = torch.randn((1, npix, npix), device=device, dtype=torch.float32)
+        lam = 1.0
+        for _ in range(12):
+            xp = plan.ms2dirty(plan.dirty2ms(xp, layout="yx"), layout="yx")
+            lam = float(torch.linalg.vector_norm(xp))
+            xp /= lam
+    lr_x = 1.0 / (2.0 * lam * 1.25)
+    a1l, a2l = a1.long(), a2.long()
 
     def gd_run(nsteps, x, g, host_obs=None):
+        """Gradient descent: the image by the 1 / L step, the gains by their
+        diagonal Newton step (per antenna and channel, the curvature is the
+        sum over its baselines of |g V_pred|^2), damped by one half and
+        capped at 0.05 per step."""
         losses = []
         for _ in range(nsteps):
             o = obs
@@ -1120,11 +1130,20 @@ def bench_autograd(args):
                 o = host_obs.to(device, non_blocking=True)
             x.grad = None
             g.grad = None
-            loss = (apply_gains(predict(x, plan), g, a1, a2) - o).abs().pow(2).sum()
+            v = predict(x, plan)
+            loss = (apply_gains(v, g, a1, a2) - o).abs().pow(2).sum()
             loss.backward()
             with torch.no_grad():
                 x -= lr_x * x.grad
-                g -= lr_g * g.grad
+                pw = v.detach().abs().pow(2).sum(-1).double()  # [rows, chan]
+                h = torch.zeros((nants, C), dtype=torch.float64, device=device)
+                h.index_add_(0, a1l, pw)
+                h.index_add_(0, a2l, pw)
+                step = g.grad / (4.0 * h.clamp_min(1e-30))
+                # at most 0.05 per step: while the image is far from the sky the
+                # gains must not absorb its error
+                step *= (0.05 / step.abs().clamp_min(0.05))
+                g -= step
             losses.append(loss.detach())
         return losses
 
@@ -1206,6 +1225,8 @@ def bench_autograd(args):
                          "image_rel_err_last": img_err,
                          "obs_dft_s": round(t_dft, 2), "obs_components": int(len(ix))},
                      checks={"dot_product_rel_to_cauchy_schwarz": dot},
+                     step_sizes={"image": lr_x, "lambda_max_AhA": lam,
+                                 "gains": "diagonal Newton, damped by 1/2, at most 0.05 a step"},
                      cpu_baseline={"value": round(step_vis / t_cpu / 1e6, 4), "unit": "Mvis/s",
                                    "cores": cores, "kind": "port",
                                    "sample": "oracle C gridder (FP64), dirty2ms + ms2dirty of "

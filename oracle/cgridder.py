@@ -87,11 +87,16 @@ class Prepared:
         else:
             self.tprime = None
         self.corr = numpy.ascontiguousarray(pl.correction().T)  # [ny][nx]
-        nb = max(2, 2 * (pl.ngy // (2 * max(pl.W, 8))))
-        self.band_h = -(-pl.ngy // nb)
-        self.nbands = -(-pl.ngy // self.band_h)
-        if self.nbands % 2:
-            self.nbands += 1
+        # bands of equal height h >= max(W, 8) dividing the grid into an even
+        # number of them: an item's support then reaches only its own band and
+        # the next, and the last band (odd) wraps into band 0 (even), so the
+        # two parity passes never write one row from two threads (a shorter
+        # last band would let the band before it wrap into band 0 as well)
+        h = max(pl.W, 8)
+        while pl.ngy % h or (pl.ngy // h) % 2:
+            h += 1
+        self.band_h = h
+        self.nbands = pl.ngy // h
 
     @classmethod
     def from_uvw(cls, uvw, freq, nx, ny, dx, dy, epsilon, do_w, sigma=2.0):

@@ -136,3 +136,18 @@ def test_rotation_oracle_matches_reference_golden():
     numpy.testing.assert_allclose(orot.simulate_point(geo["dist"], 0.01, -0.02),
                                   geo["simulate_point"], rtol=0, atol=1e-12)
 
+
+
+def test_c_gridder_threads_give_the_serial_result():
+    """The oracle's C gridder grids row bands in two parity passes; with
+    every band the same height and an even number of them, supports that
+    wrap from the last band into band 0 never race (1280-row grids at
+    sigma 1.25 once did), so any thread count gives the serial image."""
+    from oracle import cgridder
+    from tests.cases import random_problem
+    c = random_problem(seed=3, nrow=4000, nchan=2, npix=1024, pixsize=4e-4, wscale=400.0,
+                       uvscale=1200.0)
+    args = (c["uvw"], c["freq"], c["ms"][..., 0], None, 1024, 1024, 4e-4, 4e-4, 1e-5, True)
+    one = cgridder.ms2dirty(*args, nthreads=1, sigma=1.25)
+    many = cgridder.ms2dirty(*args, nthreads=8, sigma=1.25)
+    numpy.testing.assert_array_equal(one, many)
