@@ -257,12 +257,38 @@ __device__ __forceinline__ double pixel_nm1(const Geom &g, int ix, int iy) {
   return -r2 / (1.0 + sqrt(1.0 - r2));
 }
 
-// Phase (in turns, reduced to [-1/2, 1/2]) of w-plane k at offset tprime.
-__device__ __forceinline__ double plane_turns(const Geom &g, int k, double tprime) {
-  const double wk = g.w_lo + ((double)k - 0.5 * g.W) * g.dw;
-  const double ph = wk * tprime;
-  return ph - rint(ph);
+// frac(x) as 64-bit fixed-point turns (x in turns, FP64).
+__device__ __forceinline__ unsigned long long fixed_turns(double x) {
+  const double f = x - floor(x);  // [0, 1]; 1 wraps to 0 below
+  return ((unsigned long long)(f * 9223372036854775808.0)) << 1;
 }
+
+// The w-screen phases of planes b0, b0 + 1, ... at one pixel (plane k sits at
+// w_k = w_lo + (k - W/2) dw; its phase at offset t' = n - 1 - tc is w_k t'
+// turns): plane b0's phase w_b0 t' and the step dw t' are formed once in FP64 and held as
+// 64-bit fixed-point turns, so plane b0 + j's phase is an exact integer sum
+// (no FP64 instruction per plane; on this part a warp's FP64 instruction
+// costs 16 cycles of the SM's FP64 pipe), exact to the FP64 rounding of the
+// two products.
+struct PlaneTurns {
+  unsigned long long a, d;
+  __device__ __forceinline__ void start(const Geom &g, int b0, double tprime) {
+    const double wk = g.w_lo + ((double)b0 - 0.5 * g.W) * g.dw;
+    a = fixed_turns(wk * tprime);
+    d = fixed_turns(g.dw * tprime);
+  }
+  // turns of plane b0 + j in [-1/2, 1/2)
+  __device__ __forceinline__ float turns_f32(int j) const {
+    const unsigned long long ph = a + (unsigned long long)(unsigned)j * d;
+    return (float)(int)(unsigned)(ph >> 32) * 0x1p-32f;
+  }
+  __device__ __forceinline__ double turns_f64(int j) const {
+    const unsigned long long ph = a + (unsigned long long)(unsigned)j * d;
+    return (double)(long long)ph * 0x1p-64;
+  }
+  __device__ __forceinline__ float turns(int j, float) const { return turns_f32(j); }
+  __device__ __forceinline__ double turns(int j, double) const { return turns_f64(j); }
+};
 
 // ---------------------------------------------------------------------
 // Tile kernels: lane map and shared-memory layout.

@@ -405,11 +405,11 @@ __global__ void __launch_bounds__(kThreads)
     for (int p = 0; p < NP; ++p) a[p] = first ? (R)0 : acc[p * npix + i];
     const size_t gi = (size_t)(iy + oy) * g.ngx + (ix + ox);
     if (g.do_w) {
-      const double tp = tprime[i];
+      PlaneTurns pt;
+      pt.start(g, b0, tprime[i]);
       for (int j = 0; j < nb; ++j) {
-        const double turns = plane_turns(g, b0 + j, tp);
         R s, c;
-        sincos_2pi((R)turns, &s, &c);
+        sincos_2pi(pt.turns(j, (R)0), &s, &c);
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
           const C v = grid[((size_t)j * NP + p) * plane + gi];

@@ -94,9 +94,10 @@ int plan_geometry(const gb_plan_params *p, double w_lo, double w_hi, Geom &g) {
     return GB_ERR_INVALID_ARG;
   }
   if (p->sigma > 0.0) return plan_geometry_sigma(p, w_lo, w_hi, p->sigma, g);
-  // sigma 0: the tabulated oversampling of least modelled cost; 2.0 unless
-  // another is at least 10 % cheaper (power-of-two grids for power-of-two
-  // images, the library's own transforms)
+  // sigma 0: the tabulated oversampling of least modelled cost among those
+  // the form allows; 2.0 unless another is at least 10 % cheaper
+  // (power-of-two grids for power-of-two images, the library's own
+  // transforms)
   static const double kSigmas[] = {2.0, 1.75, 1.5, 1.25};
   double best = 0.0;
   bool found = false;
@@ -148,6 +149,17 @@ static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi
   if (p->precision == GB_FP32 && p->epsilon < 1e-6) {
     set_error("epsilon %g is below what the FP32 form can reach (1e-6); use GB_FP64",
               p->epsilon);
+    return GB_ERR_INVALID_ARG;
+  }
+  // At sigma 1.25 the kernel's Fourier transform falls to 0.7 % of its peak at
+  // the image edge, so the correction multiplies edge pixels by up to ~150 per
+  // dimension: FP32 grid rounding (and the run-to-run order of its float
+  // atomics) then reaches 1e-4 there.  The FP32 form keeps sigma >= 1.5 below
+  // epsilon 1e-4.
+  if (p->precision == GB_FP32 && sigma < 1.5 && p->epsilon < 1e-4) {
+    set_error("sigma %g with epsilon %g: the FP32 form needs sigma >= 1.5 (its grid rounding, "
+              "amplified by the edge correction, exceeds epsilon); use GB_FP64 or sigma >= 1.5",
+              sigma, p->epsilon);
     return GB_ERR_INVALID_ARG;
   }
   if (!std::isfinite(w_lo) || !std::isfinite(w_hi) || w_hi < w_lo) {
@@ -502,11 +514,6 @@ __global__ void k_slab_items(const uint32_t *__restrict__ offsets, int nslabs, i
 // Correction image [ny][nx]: 1/(phihat_u phihat_v) and, with w-stacking,
 // 1/(phihat_w(dw t') n).  phihat_w by Gauss-Legendre quadrature of the
 // (even) kernel on [0, W/2].
-// frac(x) as 64-bit fixed-point turns (x in turns, FP64).
-__device__ __forceinline__ unsigned long long fixed_turns(double x) {
-  const double f = x - floor(x);  // [0, 1]; 1 wraps to 0 below
-  return ((unsigned long long)(f * 9223372036854775808.0)) << 1;
-}
 
 template <typename R>
 __global__ void k_corr_image(const Geom g, const double *__restrict__ cu,

@@ -71,11 +71,11 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
       for (int p = 0; p < NP; ++p) v[p] = img[p * npix + pi];
       if (g.do_w) {
-        const double tp = tprime[pi];
+        PlaneTurns pt;
+        pt.start(g, b0, tprime[pi]);
         for (int j = 0; j < nb; ++j) {
-          const double turns = plane_turns(g, b0 + j, tp);
           R s, c;
-          sincos_2pi((R)turns, &s, &c);
+          sincos_2pi(pt.turns(j, (R)0), &s, &c);
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
             C z;
@@ -318,6 +318,10 @@ __host__ __device__ constexpr int lane_row(int NP, int SW) {
   return (SW | 1) * NP + (NP == 4 ? 2 : 0);
 }
 
+// Pols summed per staging pass of k_degrid_lane: two for NP = 4 (half the
+// staging and per-thread sums, so more CTAs fit an SM), else all.
+__host__ __device__ constexpr int degrid_pass_pols(int NP) { return NP == 4 ? 2 : NP; }
+
 // FP32 degridder, one item per thread.  A CTA takes a chunk (up to 256
 // items of one bucket); thread i owns item i: its u and v kernel values
 // (with the checkerboard sign (-1)^(p+q) folded in) stay in registers for
@@ -341,8 +345,9 @@ __device__ __forceinline__ void degrid_lane_chunk(
     const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
     const float *__restrict__ wgt, const PolMat &pm, const RowPerm &rp, float2 *stage,
     float *skv) {
+  constexpr int PP = degrid_pass_pols(NP);
   const int T = g.T;
-  const int SW = T + WT - 1, rowf2 = lane_row(NP, SW), pstride = SW * rowf2;
+  const int SW = T + WT - 1, rowf2 = lane_row(PP, SW), pstride = SW * rowf2;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   (void)lane;
   const float scale_u = 2.f / (float)WT;
@@ -372,102 +377,109 @@ __device__ __forceinline__ void degrid_lane_chunk(
       ku[a] = ((lu + a + tpar) & 1) ? -x : x;
       skv[a * kThreads + threadIdx.x] = ((lv + a) & 1) ? -y : y;
     }
-    // raw sub-grid of plane k -> dst, as one cp.async commit group per thread
-    auto stage_plane = [&](int k, float2 *dst) {
-      const float2 *gp = grid + (int64_t)(k - b0) * NP * plane;
-      for (int r = warp; r < NP * SW; r += kWarps) {
-        const int pol = r / SW, y = r - pol * SW;
-        int q = tv * T + y;
-        while (q >= g.ngy) q -= g.ngy;
-        const float2 *src = gp + pol * plane + (int64_t)rp.row(q) * g.ngx;
-        float2 *d = dst + y * rowf2 + pol;
-        for (int x = lane; x < SW; x += 32) {
-          int pc = tu * T + x;
-          while (pc >= g.ngx) pc -= g.ngx;
-          cp_async8(d + x * NP, src + pc, true);
-        }
-      }
-      cp_async_commit();
-    };
-    if (!direct && k_lo < k_hi) stage_plane(k_lo, stage);
     float2 acc[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
-    for (int k = k_lo; k < k_hi; ++k) {
-      const float2 *gp = grid + (int64_t)(k - b0) * NP * plane;
-      const float2 *sg = stage + ((k - k_lo) & 1) * pstride;
-      if (!direct) {
-        // plane k + 1 goes to the other buffer (consumed in iteration k - 1,
-        // released by that iteration's closing barrier)
-        if (k + 1 < k_hi) {
-          stage_plane(k + 1, stage + ((k + 1 - k_lo) & 1) * pstride);
-          cp_async_wait1();
-        } else {
-          cp_async_wait0();
+    // the pols in passes of PP: each pass stages its pols' sub-grids only,
+    // which halves the staging buffers and the per-thread sums for NP = 4
+    // (unrolled: acc stays in registers)
+#pragma unroll
+    for (int pb = 0; pb < NP; pb += PP) {
+      // raw sub-grid of plane k (pols pb .. pb + PP) -> dst, one cp.async
+      // commit group per thread
+      auto stage_plane = [&](int k, float2 *dst) {
+        const float2 *gp = grid + ((int64_t)(k - b0) * NP + pb) * plane;
+        for (int r = warp; r < PP * SW; r += kWarps) {
+          const int pol = r / SW, y = r - pol * SW;
+          int q = tv * T + y;
+          while (q >= g.ngy) q -= g.ngy;
+          const float2 *src = gp + pol * plane + (int64_t)rp.row(q) * g.ngx;
+          float2 *d = dst + y * rowf2 + pol;
+          for (int x = lane; x < SW; x += 32) {
+            int pc = tu * T + x;
+            while (pc >= g.ngx) pc -= g.ngx;
+            cp_async8(d + x * PP, src + pc, true);
+          }
         }
-        __syncthreads();  // plane k staged by every thread
-      }
-      const int aw = k - k0;
-      if (has && aw >= 0 && aw < wk) {
-        const float fw = g.do_w ? es_kernel(((float)aw - it.dwf) * scale_u, beta) : 1.f;
-        float2 sum[NP];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) sum[p] = make_float2(0.f, 0.f);
-#pragma unroll 1
-        for (int b = 0; b < WT; ++b) {
-          float2 rs[NP];
-#pragma unroll
-          for (int p = 0; p < NP; ++p) rs[p] = make_float2(0.f, 0.f);
-          if (direct) {
-            int q = tv * T + lv + b;
-            while (q >= g.ngy) q -= g.ngy;
-            const float2 *row = gp + (int64_t)rp.row(q) * g.ngx;
-#pragma unroll
-            for (int a = 0; a < WT; ++a) {
-              int pc = tu * T + lu + a;
-              while (pc >= g.ngx) pc -= g.ngx;
-#pragma unroll
-              for (int p = 0; p < NP; ++p) {
-                const float2 v = row[p * plane + pc];
-                rs[p].x += ku[a] * v.x;
-                rs[p].y += ku[a] * v.y;
-              }
-            }
+        cp_async_commit();
+      };
+      if (!direct && k_lo < k_hi) stage_plane(k_lo, stage);
+      for (int k = k_lo; k < k_hi; ++k) {
+        const float2 *gp = grid + ((int64_t)(k - b0) * NP + pb) * plane;
+        const float2 *sg = stage + ((k - k_lo) & 1) * pstride;
+        if (!direct) {
+          // plane k + 1 goes to the other buffer (consumed in iteration k - 1,
+          // released by that iteration's closing barrier)
+          if (k + 1 < k_hi) {
+            stage_plane(k + 1, stage + ((k + 1 - k_lo) & 1) * pstride);
+            cp_async_wait1();
           } else {
-            // a cell's NP values are contiguous: 16-byte loads of two pols
-            const float2 *row = sg + (lv + b) * rowf2 + lu * NP;
+            cp_async_wait0();
+          }
+          __syncthreads();  // plane k staged by every thread
+        }
+        const int aw = k - k0;
+        if (has && aw >= 0 && aw < wk) {
+          const float fw = g.do_w ? es_kernel(((float)aw - it.dwf) * scale_u, beta) : 1.f;
+          float2 sum[PP];
 #pragma unroll
-            for (int a = 0; a < WT; ++a) {
-              if constexpr (NP == 1) {
-                const float2 v = row[a];
-                rs[0].x += ku[a] * v.x;
-                rs[0].y += ku[a] * v.y;
-              } else {
+          for (int p = 0; p < PP; ++p) sum[p] = make_float2(0.f, 0.f);
+#pragma unroll 1
+          for (int b = 0; b < WT; ++b) {
+            float2 rs[PP];
 #pragma unroll
-                for (int pp = 0; pp < NP / 2; ++pp) {
-                  const float4 v = *reinterpret_cast<const float4 *>(row + a * NP + 2 * pp);
-                  rs[2 * pp].x += ku[a] * v.x;
-                  rs[2 * pp].y += ku[a] * v.y;
-                  rs[2 * pp + 1].x += ku[a] * v.z;
-                  rs[2 * pp + 1].y += ku[a] * v.w;
+            for (int p = 0; p < PP; ++p) rs[p] = make_float2(0.f, 0.f);
+            if (direct) {
+              int q = tv * T + lv + b;
+              while (q >= g.ngy) q -= g.ngy;
+              const float2 *row = gp + (int64_t)rp.row(q) * g.ngx;
+#pragma unroll
+              for (int a = 0; a < WT; ++a) {
+                int pc = tu * T + lu + a;
+                while (pc >= g.ngx) pc -= g.ngx;
+#pragma unroll
+                for (int p = 0; p < PP; ++p) {
+                  const float2 v = row[p * plane + pc];
+                  rs[p].x += ku[a] * v.x;
+                  rs[p].y += ku[a] * v.y;
+                }
+              }
+            } else {
+              // a cell's PP values are contiguous: 16-byte loads of two pols
+              const float2 *row = sg + (lv + b) * rowf2 + lu * PP;
+#pragma unroll
+              for (int a = 0; a < WT; ++a) {
+                if constexpr (PP == 1) {
+                  const float2 v = row[a];
+                  rs[0].x += ku[a] * v.x;
+                  rs[0].y += ku[a] * v.y;
+                } else {
+#pragma unroll
+                  for (int pp = 0; pp < PP / 2; ++pp) {
+                    const float4 v = *reinterpret_cast<const float4 *>(row + a * PP + 2 * pp);
+                    rs[2 * pp].x += ku[a] * v.x;
+                    rs[2 * pp].y += ku[a] * v.y;
+                    rs[2 * pp + 1].x += ku[a] * v.z;
+                    rs[2 * pp + 1].y += ku[a] * v.w;
+                  }
                 }
               }
             }
-          }
-          const float kvb = skv[b * kThreads + threadIdx.x];
+            const float kvb = skv[b * kThreads + threadIdx.x];
 #pragma unroll
-          for (int p = 0; p < NP; ++p) {
-            sum[p].x += kvb * rs[p].x;
-            sum[p].y += kvb * rs[p].y;
+            for (int p = 0; p < PP; ++p) {
+              sum[p].x += kvb * rs[p].x;
+              sum[p].y += kvb * rs[p].y;
+            }
+          }
+#pragma unroll
+          for (int p = 0; p < PP; ++p) {
+            acc[pb + p].x += fw * sum[p].x;
+            acc[pb + p].y += fw * sum[p].y;
           }
         }
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-          acc[p].x += fw * sum[p].x;
-          acc[p].y += fw * sum[p].y;
-        }
+        if (!direct) __syncthreads();  // buffer consumed before it is refilled
       }
-      if (!direct) __syncthreads();  // buffer consumed before it is refilled
     }
     if (has && k0 + wk > b0 && k0 < b0 + nb) {
       float2 v[NP];
@@ -512,15 +524,18 @@ __device__ __forceinline__ void degrid_lane_chunk(
   }
 }
 
+// CTAs per SM the lane degridders are compiled for (registers <= 80).
+constexpr int kDegridLaneBlocks = 3;
+
 template <int NP, int WT>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
     k_degrid_lane(const Geom g, const ItemF *__restrict__ items, const Chunk *__restrict__ chunks,
                   const uint32_t *__restrict__ chunk_off, int b0, int nb,
                   const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
                   const float *__restrict__ wgt, const PolMat pm, const RowPerm rp,
                   uint32_t *__restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int SW = g.T + WT - 1, pstride = SW * lane_row(NP, SW);
+  const int SW = g.T + WT - 1, pstride = SW * lane_row(degrid_pass_pols(NP), SW);
   float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][rowf2]
   float *skv = reinterpret_cast<float *>(stage + 2 * pstride);   // [WT][kThreads]: own kv
   const int ntiles = g.ntu * g.ntv;
@@ -546,7 +561,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 // in k_grid_jobs; each CTA takes the next index from one atomic counter and
 // degrids that chunk of its job into the job's visibilities.
 template <int NP, int WT>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
     k_degrid_lane_jobs(const __grid_constant__ GridJobs jobs, const PolMat pm,
                        uint32_t *__restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -556,7 +571,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   int pstride_max = 0;
   for (int j = 0; j < jobs.n; ++j) {
     const int SW = jobs.job[j].g.T + WT - 1;
-    pstride_max = max(pstride_max, SW * lane_row(NP, SW));
+    pstride_max = max(pstride_max, SW * lane_row(degrid_pass_pols(NP), SW));
   }
   float2 *stage = reinterpret_cast<float2 *>(smem_raw);
   float *skv = reinterpret_cast<float *>(stage + 2 * pstride_max);
@@ -603,7 +618,7 @@ __global__ void __launch_bounds__(kThreads, 2)
 
 size_t degrid_lane_smem_bytes(const gb_plan *p) {
   const int SW = p->g.T + p->g.W - 1;
-  return (size_t)2 * SW * lane_row(p->g.NP, SW) * sizeof(float2) +
+  return (size_t)2 * SW * lane_row(degrid_pass_pols(p->g.NP), SW) * sizeof(float2) +
          (size_t)p->g.W * kThreads * sizeof(float);
 }
 
@@ -849,7 +864,7 @@ int launch_degrid_jobs(const GridJobs &jobs, const PolMat &pm, int num_sms, uint
       return GB_ERR_INVALID_ARG;
     }
     const int SW = g.T + W - 1;
-    pstride = std::max(pstride, SW * lane_row(NP, SW));
+    pstride = std::max(pstride, SW * lane_row(degrid_pass_pols(NP), SW));
   }
   const size_t smem = (size_t)2 * pstride * sizeof(float2) + (size_t)W * kThreads * sizeof(float);
   ProfScope ps(kProfDegrid, s, bytes, updates);

@@ -132,8 +132,8 @@ def test_native_batch_graph_capture_and_mixed_supports():
     b.close()
     # the same list with two oversamplings forced alternately
     b2 = SnapshotBatch(snaps, 1e-5, precision="fp32", nslots=4,
-                       sigmas=[2.0 if i % 2 else 1.25 for i in range(len(snaps))])
-    assert {p.info["support"] for p in b2.plans} == {7, 11}
+                       sigmas=[2.0 if i % 2 else 1.5 for i in range(len(snaps))])
+    assert {p.info["support"] for p in b2.plans} == {7, 9}  # lane widths 8 and 16
     b2.run_native(vis, models)
     torch.cuda.synchronize()
     for i, sn in enumerate(snaps):

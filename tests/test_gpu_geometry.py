@@ -115,10 +115,29 @@ def test_wide_grid_column_mode_against_cpu_oracle(npix, own_rows):
            nrows_check=128, npix_check=32, sigma=2.0)
 
 
-@pytest.mark.parametrize("sigma", [1.25, 1.5, 1.75])
-def test_low_like_geometry_other_oversampling(sigma):
-    """The FP32 form at every other tabulated grid oversampling (batched
-    cuFFT transforms, larger supports), LOW-like baselines."""
+@pytest.mark.parametrize("precision,eps,tol,sigma", [("fp32", 1e-5, 1e-5, 1.5),
+                                                      ("fp32", 1e-5, 1e-5, 1.75),
+                                                      ("fp64", 1e-12, 1e-10, 1.25),
+                                                      ("fp64", 1e-9, 1e-8, 1.25)])
+def test_low_like_geometry_other_oversampling(precision, eps, tol, sigma):
+    """Both forms at the other tabulated grid oversamplings (batched cuFFT
+    transforms, larger supports, the w-screen phases in fixed point),
+    LOW-like baselines."""
     fu, freq, dirty, src = _geometry("low-like", 2, 2, 1024, 1e-5)
-    info = _check(fu, freq, dirty, src, 1024, 1e-5, "fp32", 1e-5, 1e-5, sigma=sigma)
+    try:
+        info = _check(fu, freq, dirty, src, 1024, 1e-5, precision, eps, tol, sigma=sigma)
+    except ValueError as e:  # epsilon out of this oversampling's reach
+        assert precision == "fp64" and eps == 1e-12 and "not reachable" in str(e)
+        return
     assert info["sigma"] == sigma and info["fft_mode"] == 1
+
+
+def test_fp32_form_refuses_sigma_125():
+    """At sigma 1.25 the edge correction amplifies FP32 grid rounding beyond
+    epsilon 1e-5, so the FP32 form refuses it (and the planner never picks it)."""
+    from rascil_gb300.wgridder import Plan
+    fu, freq, dirty, src = _geometry("low-like", 1, 1, 256, 1e-5)
+    u = torch.from_numpy(fu.copy()).cuda()
+    f = torch.from_numpy(freq.copy()).cuda()
+    with pytest.raises(ValueError, match="sigma >= 1.5"):
+        Plan(u, f, 256, 256, 1e-5, 1e-5, 1e-5, True, precision="fp32", sigma=1.25)

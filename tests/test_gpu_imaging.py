@@ -189,7 +189,9 @@ def test_plan_cache_reuse_and_invalidation(monkeypatch):
     im_n, sw_n = invert_ng(bvis, model, **kw)
     v_n = predict_ng(bvis, model, **kw)["vis"].data
     numpy.testing.assert_array_equal(sw_c, sw_n)
-    assert rel_rms(im_c["pixels"].data, im_n["pixels"].data) < 1e-6
+    # FP32 float-atomic flushes sum in a run-dependent order; the planner's
+    # wide-field oversampling (1.5 here) amplifies that at the image edge
+    assert rel_rms(im_c["pixels"].data, im_n["pixels"].data) < 1e-5
     numpy.testing.assert_array_equal(v_c, v_n)  # one thread per item: deterministic sums
     # uvw scaled in place after the cached invert: predict must see the new uvw
     monkeypatch.setenv("RASCIL_GB300_PLAN_CACHE", "1")

@@ -285,9 +285,11 @@ def test_empty_visibilities_need_no_device():
 def test_planner_geometry_matches_oracle_other_sigmas(sigma):
     from oracle import wgridder as owg
     from rascil_gb300.wgridder import plan_geometry
-    info = plan_geometry(1024, 1024, 1e-4, 1e-4, 1e-5, True, -800.0, 2500.0, precision="fp32",
+    prec = "fp64" if sigma < 1.5 else "fp32"  # the FP32 form keeps sigma >= 1.5
+    info = plan_geometry(1024, 1024, 1e-4, 1e-4, 1e-5, True, -800.0, 2500.0, precision=prec,
                          sigma=sigma)
-    op = owg.Plan(1024, 1024, 1e-4, 1e-4, 1e-5, True, -800.0, 2500.0, sigma=sigma, fp32=True)
+    op = owg.Plan(1024, 1024, 1e-4, 1e-4, 1e-5, True, -800.0, 2500.0, sigma=sigma,
+                  fp32=prec == "fp32")
     assert (info["support"], info["beta"], info["ngrid_x"], info["nplanes"], info["dw"]) == (
         op.W, op.beta, op.ngx, op.nplanes, op.dw)
 
@@ -295,13 +297,17 @@ def test_planner_geometry_matches_oracle_other_sigmas(sigma):
 def test_planner_chooses_oversampling_by_cost():
     """With sigma 0 the planner weighs gridding work (W^3 per item) against
     per-plane transform work: a wide field with few visibilities and many
-    w-planes takes the smallest oversampling, a dense narrow field (the
-    LOW-like workload) keeps sigma 2 and the library's own transforms; an
-    explicit sigma is kept."""
+    w-planes takes the smallest oversampling its form allows (1.5 for FP32,
+    whose grid rounding sigma 1.25's edge correction would amplify beyond
+    epsilon), a dense narrow field (the LOW-like workload) keeps sigma 2 and
+    the library's own transforms; an explicit sigma is kept."""
     from rascil_gb300.wgridder import plan_geometry
     wide = plan_geometry(2048, 2048, 5.8e-4, 5.8e-4, 1e-5, True, -700.0, 700.0, nrows=100000,
                          nchan=2, precision="fp32")
-    assert wide["sigma"] == 1.25 and wide["fft_mode"] == 1
+    assert wide["sigma"] == 1.5 and wide["fft_mode"] == 1  # 1.25 is below the FP32 form's
+    wide64 = plan_geometry(2048, 2048, 5.8e-4, 5.8e-4, 1e-7, True, -700.0, 700.0, nrows=100000,
+                           nchan=2, precision="fp64")
+    assert wide64["sigma"] == 1.25
     dense = plan_geometry(8192, 8192, 1e-5, 1e-5, 1e-5, True, -40000.0, 41000.0,
                           nrows=16744448, nchan=16, npol=4, precision="fp32")
     assert dense["sigma"] == 2.0 and dense["fft_mode"] == 2
