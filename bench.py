@@ -437,7 +437,7 @@ def _sample_planes(nplanes, n):
 
 
 def _items_reaching(plan, w, planes):
-    a = numpy.ceil((w - plan.w_lo) / plan.dw)
+    a = numpy.ceil((numpy.abs(w) - plan.w_lo) / plan.dw)  # w-stacking mirrors w < 0
     keep = numpy.zeros(w.size, dtype=bool)
     for k in planes:
         keep |= (a >= k - plan.W + 1) & (a <= k)
@@ -452,7 +452,7 @@ def cpu_gridder_sample(u, v, w, values, model, npix, cell, eps, nplanes_sample, 
     items gridded)."""
     from oracle import cgridder
     from oracle import wgridder as owg
-    plan = owg.Plan(npix, npix, cell, cell, eps, True, float(w.min()), float(w.max()), sigma)
+    plan = owg.Plan(npix, npix, cell, cell, eps, True, *owg.w_range(w, True), sigma)
     planes = _sample_planes(plan.nplanes, nplanes_sample)
     idx = _items_reaching(plan, w, planes)
     pr = cgridder.Prepared(plan, u[idx], v[idx], w[idx])

@@ -279,9 +279,10 @@ int gb_probe_smem_peaks(double *atomics_per_s, double *loads8_per_s, void *strea
  * instead, and calls no allocating routine.  No counterpart in the
  * reference.
  *   uvw_dev [nrows][3] metres, freq_dev [nchan] Hz (float64, device)
- *   out_dev [4] float64 (device): w_lo, w_hi in wavelengths over all (row,
- *           channel) items with a finite uvw row and a positive, finite
- *           frequency, then the number of rows with a non-finite coordinate
+ *   out_dev [4] float64 (device): w_lo, w_hi, the range of |w| in
+ *           wavelengths (a w-stacking plan mirrors rows with w < 0 to -uvw)
+ *           over all (row, channel) items with a finite uvw row and a
+ *           positive, finite frequency, then the number of rows with a non-finite coordinate
  *           and the number of non-positive or non-finite frequencies.  For
  *           input the planner accepts (both counts zero) and a w-stacking
  *           plan, w_lo and w_hi are bit-identical to gb_plan_info's; plans

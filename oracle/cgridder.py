@@ -70,7 +70,8 @@ class Prepared:
 
     def __init__(self, plan, u, v, w):
         self.plan = plan
-        p0, q0, k0, du, dv, dwf, ph = plan.coords_lambda(u, v, w)
+        p0, q0, k0, du, dv, dwf, ph, flip = plan.coords_lambda(u, v, w)
+        self.flip = flip  # mirrored items: grid conj(value), predict the conjugate
         self.p0 = numpy.ascontiguousarray(p0, dtype=numpy.int32)
         self.q0 = numpy.ascontiguousarray(q0, dtype=numpy.int32)
         self.k0 = numpy.ascontiguousarray(k0, dtype=numpy.int32)
@@ -104,7 +105,7 @@ class Prepared:
         u = (uvw[:, 0:1] * s).ravel()
         v = (uvw[:, 1:2] * s).ravel()
         w = (uvw[:, 2:3] * s).ravel()
-        plan = owg.Plan(nx, ny, dx, dy, epsilon, do_w, float(w.min()), float(w.max()), sigma)
+        plan = owg.Plan(nx, ny, dx, dy, epsilon, do_w, *owg.w_range(w, do_w), sigma)
         return cls(plan, u, v, w)
 
     def items_of_plane(self, k):
@@ -126,7 +127,8 @@ def grid_items(pr, c, nthreads=None, planes=None):
     lib = _load()
     nthreads = nthreads or max_threads()
     pl = pr.plan
-    c = numpy.ascontiguousarray(numpy.asarray(c, dtype=numpy.complex128).ravel() * pr.ph)
+    c = numpy.asarray(c, dtype=numpy.complex128).ravel()
+    c = numpy.ascontiguousarray(numpy.where(pr.flip, numpy.conj(c), c) * pr.ph)
     cv = c.view(numpy.float64)
     acc = numpy.zeros((pl.ny, pl.nx))
     grid = numpy.zeros((pl.ngy, pl.ngx), dtype=numpy.complex128)
@@ -169,7 +171,8 @@ def degrid_items(pr, image_yx, nthreads=None, planes=None):
         lib.og_degrid_plane(pl.ngx, pl.ngy, pl.W, pl.beta, int(pl.do_w), int(k), _p(pr.p0),
                             _p(pr.q0), _p(pr.k0), _p(pr.du), _p(pr.dv), _p(pr.dwf), _p(idx),
                             int(idx.size), _p(g.view(numpy.float64)), _p(ov), nthreads)
-    return out * numpy.conj(pr.ph)
+    out = out * numpy.conj(pr.ph)
+    return numpy.where(pr.flip, numpy.conj(out), out)
 
 
 def ms2dirty(uvw, freq, ms, wgt, npix_x, npix_y, pixsize_x, pixsize_y, epsilon, do_wstacking,

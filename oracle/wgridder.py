@@ -59,6 +59,13 @@ def good_size(n):
         n += 1
 
 
+def w_range(w, do_wstacking):
+    """The w range a plan spans: of |w| with w-stacking (items with w < 0
+    are mirrored, :meth:`Plan.coords_lambda`), of w otherwise."""
+    a = numpy.abs(w) if do_wstacking else numpy.asarray(w)
+    return float(a.min()), float(a.max())
+
+
 def choose_kernel(epsilon, do_wstacking, sigma=2.0, fp32=False):
     ndim = 3 if do_wstacking else 2
     if fp32 and epsilon < 1e-6:
@@ -140,39 +147,24 @@ class Plan:
 
     # -- per-visibility coordinates -------------------------------------
     def coords(self, uvw, freq):
-        """Per (row, chan) item: p0, q0 (wrapped), k0, du, dv, dwf, phase."""
+        """Per (row, chan) item: p0, q0 (wrapped), k0, du, dv, dwf, phase,
+        flip (see :meth:`coords_lambda`)."""
         s = numpy.asarray(freq, dtype=numpy.float64) / SPEED_OF_LIGHT
-        u = uvw[:, 0:1] * s
-        v = uvw[:, 1:2] * s
-        w = uvw[:, 2:3] * s
-        W = self.W
-        fu = u * self.dx
-        fu = fu - numpy.floor(fu)
-        U = fu * self.ngx
-        p0 = numpy.ceil(U - 0.5 * W)
-        du = U - p0
-        fv = v * self.dy
-        fv = fv - numpy.floor(fv)
-        V = fv * self.ngy
-        q0 = numpy.ceil(V - 0.5 * W)
-        dv = V - q0
-        p0 = numpy.mod(p0.astype(numpy.int64), self.ngx)
-        q0 = numpy.mod(q0.astype(numpy.int64), self.ngy)
-        if self.do_w:
-            a = (w - self.w_lo) / self.dw
-            k0 = numpy.ceil(a)
-            dwf = a - k0 + 0.5 * W
-            k0 = numpy.clip(k0.astype(numpy.int64), 0, self.nplanes - W)
-            phase = numpy.exp(-2j * numpy.pi * w * self.tc)
-        else:
-            k0 = numpy.zeros(u.shape, dtype=numpy.int64)
-            dwf = numpy.zeros(u.shape)
-            phase = numpy.ones(u.shape, dtype=numpy.complex128)
-        return p0, q0, k0, du, dv, dwf, phase
+        return self.coords_lambda(uvw[:, 0:1] * s, uvw[:, 1:2] * s, uvw[:, 2:3] * s)
 
     def coords_lambda(self, u, v, w):
-        """Like :meth:`coords` for per-item u, v, w already in wavelengths."""
+        """Per item with u, v, w in wavelengths: p0, q0 (wrapped), k0, du, dv,
+        dwf, phase and flip.  With w-stacking, items with w < 0 are mirrored
+        to (-u, -v, -w) (flip True): every image is real, so such an item
+        grids conj(value) and predicts the conjugate (Hermitian symmetry),
+        and the w range spans |w| only (half the w-planes of a range
+        symmetric about zero)."""
         W = self.W
+        if self.do_w:
+            flip = w < 0.0
+            u, v, w = (numpy.where(flip, -x, x) for x in (u, v, w))
+        else:
+            flip = numpy.zeros(numpy.broadcast(u, v, w).shape, dtype=bool)
         fu = u * self.dx
         fu = fu - numpy.floor(fu)
         U = fu * self.ngx
@@ -195,7 +187,7 @@ class Plan:
             k0 = numpy.zeros(u.shape, dtype=numpy.int64)
             dwf = numpy.zeros(u.shape)
             phase = numpy.ones(u.shape, dtype=numpy.complex128)
-        return p0, q0, k0, du, dv, dwf, phase
+        return p0, q0, k0, du, dv, dwf, phase, flip
 
     def weights(self, du, dv, dwf):
         """Kernel values [n, W] for u, v and (if w-stacking) w."""
@@ -217,12 +209,12 @@ def ms2dirty(uvw, freq, ms, wgt, npix_x, npix_y, pixsize_x, pixsize_y, epsilon,
     s = numpy.asarray(freq, dtype=numpy.float64) / SPEED_OF_LIGHT
     w_all = uvw[:, 2:3] * s
     plan = Plan(npix_x, npix_y, pixsize_x, pixsize_y, epsilon, do_wstacking,
-                float(w_all.min()), float(w_all.max()), sigma, support=support)
-    p0, q0, k0, du, dv, dwf, phase = (x.ravel() for x in plan.coords(uvw, freq))
+                *w_range(w_all, do_wstacking), sigma, support=support)
+    p0, q0, k0, du, dv, dwf, phase, flip = (x.ravel() for x in plan.coords(uvw, freq))
     c = numpy.asarray(ms, dtype=numpy.complex128).ravel()
     if wgt is not None:
         c = c * numpy.asarray(wgt, dtype=numpy.float64).ravel()
-    c = c * phase
+    c = numpy.where(flip, numpy.conj(c), c) * phase
     ku, kv, kw = plan.weights(du, dv, dwf)
     W = plan.W
     acc = numpy.zeros((npix_x, npix_y))
@@ -257,8 +249,8 @@ def dirty2ms(uvw, freq, dirty, wgt, pixsize_x, pixsize_y, epsilon, do_wstacking,
     s = numpy.asarray(freq, dtype=numpy.float64) / SPEED_OF_LIGHT
     w_all = uvw[:, 2:3] * s
     plan = Plan(npix_x, npix_y, pixsize_x, pixsize_y, epsilon, do_wstacking,
-                float(w_all.min()), float(w_all.max()), sigma, support=support)
-    p0, q0, k0, du, dv, dwf, phase = (x.ravel() for x in plan.coords(uvw, freq))
+                *w_range(w_all, do_wstacking), sigma, support=support)
+    p0, q0, k0, du, dv, dwf, phase, flip = (x.ravel() for x in plan.coords(uvw, freq))
     ku, kv, kw = plan.weights(du, dv, dwf)
     W = plan.W
     out = numpy.zeros(p0.size, dtype=numpy.complex128)
@@ -285,6 +277,7 @@ def dirty2ms(uvw, freq, dirty, wgt, pixsize_x, pixsize_y, epsilon, do_wstacking,
                 acc += grid[qq, pp] * ku[sel, a] * kv[sel, b] * sign
         out[sel] += acc * kw[sel, aw[sel]]
     out = out * numpy.conj(phase)
+    out = numpy.where(flip, numpy.conj(out), out)
     out = out.reshape(uvw.shape[0], len(freq))
     if wgt is not None:
         out = out * wgt

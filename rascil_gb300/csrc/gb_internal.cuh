@@ -58,10 +58,13 @@ struct Geom {
 };
 
 // Item record in bucket order.  `loc` packs the item's first support cell
-// inside its tile (bits 0-7 u, 8-15 v) and its first w-plane inside its
-// slab (bits 16-23).  du, dv, dwf are the offsets of the item's continuous
-// grid coordinate from its first support cell (in (W/2-1, W/2]); ph is
-// exp(-2 pi i w tc), the rotation that centres the (n-1) band.
+// inside its tile (bits 0-7 u, 8-15 v), its first w-plane inside its
+// slab (bits 16-23) and whether it is mirrored to -uvw (bit 31, kLocFlip:
+// invert grids conj(value), predict conjugates its result).  du, dv, dwf
+// are the offsets of the item's continuous grid coordinate from its first
+// support cell (in (W/2-1, W/2]); ph is exp(-2 pi i w tc), the rotation
+// that centres the (n-1) band (w after the mirroring).
+constexpr uint32_t kLocFlip = 0x80000000u;
 struct __align__(16) ItemF {
   uint32_t idx, loc;
   float du, dv, dwf, pad;
@@ -130,8 +133,9 @@ template <> __device__ __forceinline__ double pm_im<double>(const PolMat &pm, in
 struct Coord {
   int p0, q0;      // first support cell, wrapped into [0, ng)
   int k0;          // first w-plane
+  int flip;        // the item is mirrored to -uvw (see row_flipped)
   double du, dv, dwf;
-  double w;        // w in wavelengths
+  double w;        // w in wavelengths (after the mirroring)
 };
 
 __host__ __device__ inline double gb_mul(double a, double b) {
@@ -163,6 +167,18 @@ __host__ __device__ inline double gb_div(double a, double b) {
 #endif
 }
 
+// Hermitian mirroring.  Every image the gridder makes or reads is real
+// (ms2dirty keeps the real part; dirty2ms takes a real image), so an item at
+// (u, v, w) with value V contributes exactly what an item at (-u, -v, -w)
+// with value conj(V) does, and the prediction at -uvw is the conjugate of
+// the one at uvw.  With w-stacking, rows with w < 0 are mirrored: the w
+// range then spans |w| only, which halves the number of w-planes (and their
+// transforms) for a w range symmetric about zero.  Negation is exact, so a
+// mirrored coordinate is bit-identical to the product formed from -uvw.
+__host__ __device__ inline bool row_flipped(const Geom &g, const double *uvw, uint32_t r) {
+  return g.do_w && uvw[3 * (size_t)r + 2] < 0.0;
+}
+
 // Turns of an item's rotation factor exp(-2 pi i turns), reduced to
 // [-1/2, 1/2]: the w-centring term w tc and, when `shift`, minus the fused
 // phase shift (u, v, w) . s (wavelengths).  Formed in FP64 before the
@@ -172,11 +188,12 @@ __host__ __device__ inline double item_turns(const Geom &g, const double *uvw,
   const uint32_t r = i / (uint32_t)g.C;
   const uint32_t c = i - r * (uint32_t)g.C;
   const double k = gb_div(freq[c], kSpeedOfLight);
-  const double w = gb_mul(uvw[3 * (size_t)r + 2], k);
+  const double sg = row_flipped(g, uvw, r) ? -1.0 : 1.0;  // exact: a sign change
+  const double w = sg * gb_mul(uvw[3 * (size_t)r + 2], k);
   double t = g.do_w ? gb_mul(w, g.tc) : 0.0;
   if (shift) {
-    const double u = gb_mul(uvw[3 * (size_t)r + 0], k);
-    const double v = gb_mul(uvw[3 * (size_t)r + 1], k);
+    const double u = sg * gb_mul(uvw[3 * (size_t)r + 0], k);
+    const double v = sg * gb_mul(uvw[3 * (size_t)r + 1], k);
     const double d = gb_add(gb_add(gb_mul(u, g.shift[0]), gb_mul(v, g.shift[1])),
                             gb_mul(w, g.shift[2]));
     t = gb_sub(t, d);
@@ -190,9 +207,11 @@ __host__ __device__ inline void item_coord(const Geom &g, const double *uvw,
   const uint32_t r = i / (uint32_t)g.C;
   const uint32_t c = i - r * (uint32_t)g.C;
   const double s = gb_div(freq[c], kSpeedOfLight);
-  const double u = gb_mul(uvw[3 * (size_t)r + 0], s);
-  const double v = gb_mul(uvw[3 * (size_t)r + 1], s);
-  const double w = gb_mul(uvw[3 * (size_t)r + 2], s);
+  o.flip = row_flipped(g, uvw, r) ? 1 : 0;
+  const double sg = o.flip ? -1.0 : 1.0;  // exact: a sign change
+  const double u = sg * gb_mul(uvw[3 * (size_t)r + 0], s);
+  const double v = sg * gb_mul(uvw[3 * (size_t)r + 1], s);
+  const double w = sg * gb_mul(uvw[3 * (size_t)r + 2], s);
   const double halfW = 0.5 * g.W;
   double fu = gb_mul(u, g.dx);
   fu = gb_sub(fu, floor(fu));

@@ -91,11 +91,13 @@ __global__ void __launch_bounds__(kThreads)
         }
       }
     }
+    // a mirrored item (at -uvw) grids the conjugate value
+    const R conj_sign = (it.loc & kLocFlip) ? (R)-1 : (R)1;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
       const R w = (wgt ? wgt[base + p] : (R)1) * m[p];
       wsum[p] += (double)w;
-      const R re = out[p].x * w, im = out[p].y * w;
+      const R re = out[p].x * w, im = out[p].y * w * conj_sign;
       C o;
       o.x = re * ph.x - im * ph.y;
       o.y = re * ph.y + im * ph.x;

@@ -29,8 +29,9 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) double g_wrange_scratch[3 * kNoAllocMaxParts];
 
-// One block per run of kNoAllocRowsPerPart rows: min/max of w over the
-// finite rows and the number of rows holding a non-finite coordinate.
+// One block per run of kNoAllocRowsPerPart rows: min/max of |w| over the
+// finite rows (a w-stacking plan mirrors rows with w < 0 to -uvw, so its w
+// range spans |w|) and the number of rows holding a non-finite coordinate.
 __global__ void k_wrange_parts(const double *__restrict__ uvw, int64_t nrows,
                                double *__restrict__ parts) {
   const int64_t r0 = (int64_t)blockIdx.x * kNoAllocRowsPerPart;
@@ -42,8 +43,8 @@ __global__ void k_wrange_parts(const double *__restrict__ uvw, int64_t nrows,
       bad += 1.0;
       continue;
     }
-    lo = fmin(lo, w);
-    hi = fmax(hi, w);
+    lo = fmin(lo, fabs(w));
+    hi = fmax(hi, fabs(w));
   }
   for (int o = 16; o > 0; o >>= 1) {
     lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));

@@ -373,7 +373,9 @@ int scan_exclusive(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
 // ---------------------------------------------------------------------
 // w range
 
-__global__ void k_wrange(const double *__restrict__ uvw, int64_t nrows,
+// Range of w (of |w| when rows with w < 0 are mirrored, row_flipped) over
+// the finite rows, and the count of rows with a non-finite coordinate.
+__global__ void k_wrange(const double *__restrict__ uvw, int64_t nrows, int mirror,
                          double *__restrict__ part) {
   double lo = INFINITY, hi = -INFINITY, bad = 0.0;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows;
@@ -383,8 +385,9 @@ __global__ void k_wrange(const double *__restrict__ uvw, int64_t nrows,
       bad += 1.0;
       continue;
     }
-    lo = fmin(lo, w);
-    hi = fmax(hi, w);
+    const double wm = mirror ? fabs(w) : w;
+    lo = fmin(lo, wm);
+    hi = fmax(hi, wm);
   }
   for (int o = 16; o > 0; o >>= 1) {
     lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
@@ -458,7 +461,7 @@ __global__ void k_scatter(const Geom g, const double *__restrict__ uvw,
     it.idx = (uint32_t)i;
     const uint32_t lu = (uint32_t)(o.p0 % g.T), lv = (uint32_t)(o.q0 % g.T);
     const uint32_t lk = (uint32_t)(o.k0 % g.S);
-    it.loc = lu | (lv << 8) | (lk << 16);
+    it.loc = lu | (lv << 8) | (lk << 16) | (o.flip ? kLocFlip : 0u);
     it.du = (R)o.du;
     it.dv = (R)o.dv;
     it.dwf = (R)o.dwf;
@@ -1086,7 +1089,8 @@ int gb_plan_create(const gb_plan_params *params, const double *uvw_dev,
     cudaError_t le;
     {
       ProfScope ps(kProfWrange, s, 24.0 * (double)params->nrows);
-      k_wrange<<<blocks, kThreads, 0, s>>>(uvw_dev, params->nrows, part);
+      k_wrange<<<blocks, kThreads, 0, s>>>(uvw_dev, params->nrows,
+                                           params->do_wstacking ? 1 : 0, part);
       le = cudaGetLastError();
     }
     std::vector<double> hp(3 * blocks);

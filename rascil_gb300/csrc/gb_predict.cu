@@ -271,10 +271,12 @@ __global__ void __launch_bounds__(kThreads)
       const int k0 = kbase + (int)((it.loc >> 16) & 0xffu);
       if (k0 + wk > b0 && k0 < b0 + nb) {
         C v[NP];
+        // a mirrored item (at -uvw) predicts the conjugate
+        const R conj_sign = (it.loc & kLocFlip) ? (R)-1 : (R)1;
 #pragma unroll
         for (int p = 0; p < NP; ++p) {  // multiply by conj(ph) = exp(+2 pi i w tc)
           v[p].x = ar[p] * it.ph.x + ai[p] * it.ph.y;
-          v[p].y = ai[p] * it.ph.x - ar[p] * it.ph.y;
+          v[p].y = (ai[p] * it.ph.x - ar[p] * it.ph.y) * conj_sign;
         }
         const size_t base = (size_t)it.idx * npv;
         const bool first = k0 >= b0;
@@ -483,10 +485,12 @@ __device__ __forceinline__ void degrid_lane_chunk(
     }
     if (has && k0 + wk > b0 && k0 < b0 + nb) {
       float2 v[NP];
+      // a mirrored item (at -uvw) predicts the conjugate
+      const float conj_sign = (it.loc & kLocFlip) ? -1.f : 1.f;
 #pragma unroll
       for (int p = 0; p < NP; ++p) {  // multiply by conj(ph) = exp(+2 pi i w tc)
         v[p].x = acc[p].x * it.ph.x + acc[p].y * it.ph.y;
-        v[p].y = acc[p].y * it.ph.x - acc[p].x * it.ph.y;
+        v[p].y = (acc[p].y * it.ph.x - acc[p].x * it.ph.y) * conj_sign;
       }
       const size_t base = (size_t)it.idx * npv;
       const bool first = k0 >= b0;

@@ -43,10 +43,11 @@ def test_bucket_keys_bit_exact(precision, do_w):
     s = c["freq"] / dft.SPEED_OF_LIGHT
     w_all = c["uvw"][:, 2:3] * s
     op = owg.Plan(c["npix"], c["npix"], c["pixsize"], c["pixsize"], eps, do_w,
-                  float(w_all.min()), float(w_all.max()), fp32=precision == "fp32")
+                  *owg.w_range(w_all, do_w), fp32=precision == "fp32")
     assert (op.W, op.ngx, op.nplanes) == (info["support"], info["ngrid_x"], info["nplanes"])
     assert op.dw == info["dw"] and op.tc == info["tc"]
-    p0, q0, k0, du, dv, dwf, _ = (x.ravel() for x in op.coords(c["uvw"], c["freq"]))
+    p0, q0, k0, du, dv, dwf, _, flip = (x.ravel() for x in op.coords(c["uvw"], c["freq"]))
+    assert flip.any() == do_w  # with w-stacking the rows with w < 0 are mirrored
     cell = cell.cpu().numpy()
     numpy.testing.assert_array_equal(cell[:, 0], p0)
     numpy.testing.assert_array_equal(cell[:, 1], q0)
