@@ -50,6 +50,10 @@ SCALES = {
     # name: overrides of the configuration (None = as specified)
     "full": dict(ntimes=None, nchan=None, npixel=None),
     "medium": dict(ntimes=16, nchan=8, npixel=2048),
+    # the medium visibilities at twice the image side: about the full
+    # workload's items per (w-slab, uv-tile) bucket (buckets grow as the
+    # fourth power of the image side, tiles and w-planes each as its square)
+    "medium-wide": dict(ntimes=16, nchan=8, npixel=4096),
     "small": dict(ntimes=8, nchan=4, npixel=2048),
     "tiny": dict(ntimes=2, nchan=2, npixel=512),
 }
@@ -449,7 +453,13 @@ def cpu_gridder_sample(u, v, w, values, model, npix, cell, eps, nplanes_sample, 
     reaches an evenly spread subset of the w-planes: u, v, w in wavelengths
     (ng.py's sign flips applied), ``values(idx)`` gives those items' complex
     values, ``model`` is the [y][x] image.  Returns (seconds, plan, planes,
-    items gridded)."""
+    items gridded, estimated seconds of the whole invert + predict).
+
+    The estimate scales the two parts of the measured time separately: the
+    per-plane transforms and screens by (all planes / sampled planes), the
+    spreading and gathering by (all item-planes / sampled item-planes),
+    every item reaching W planes -- the sampled planes may hold more or
+    fewer items than the average plane."""
     from oracle import cgridder
     from oracle import wgridder as owg
     plan = owg.Plan(npix, npix, cell, cell, eps, True, *owg.w_range(w, True), sigma)
@@ -457,10 +467,17 @@ def cpu_gridder_sample(u, v, w, values, model, npix, cell, eps, nplanes_sample, 
     idx = _items_reaching(plan, w, planes)
     pr = cgridder.Prepared(plan, u[idx], v[idx], w[idx])
     vals = values(idx)
+    timing = {}
     t0 = time.perf_counter()
-    cgridder.grid_items(pr, vals, cores, planes)
-    cgridder.degrid_items(pr, model, cores, planes)
-    return time.perf_counter() - t0, plan, planes, idx.size
+    cgridder.grid_items(pr, vals, cores, planes, timing)
+    cgridder.degrid_items(pr, model, cores, planes, timing)
+    dt = time.perf_counter() - t0
+    est = dt * plan.nplanes / len(planes)  # fallback: plane scaling alone
+    if timing.get("item_planes"):
+        est = (timing.get("planes", 0.0) * plan.nplanes / len(planes)
+               + timing["items"] * (2.0 * w.size * plan.W) / timing["item_planes"]
+               + (dt - timing.get("planes", 0.0) - timing["items"]))
+    return dt, plan, planes, idx.size, est
 
 
 def cpu_choose_sigma(u, v, w, npix, cell, eps, cores, nplanes_probe=2, sigmas=CPU_SIGMAS):
@@ -473,12 +490,12 @@ def cpu_choose_sigma(u, v, w, npix, cell, eps, cores, nplanes_probe=2, sigmas=CP
     model = numpy.zeros((npix, npix))
     for sg in sigmas:
         try:
-            dt, plan, planes, _ = cpu_gridder_sample(
+            _, plan, planes, _, full = cpu_gridder_sample(
                 u, v, w, lambda idx: numpy.ones(idx.size, numpy.complex128), model, npix, cell,
                 eps, nplanes_probe, sg, cores)
         except (ValueError, IndexError):
             continue  # no kernel reaches eps at this sigma
-        est[sg] = dt * plan.nplanes / len(planes)
+        est[sg] = full
     if not est:
         raise ValueError("no CPU gridder oversampling reaches epsilon %g" % eps)
     return min(est, key=est.get), est
@@ -514,10 +531,11 @@ def cpu_sample(cw, nplanes_sample):
         return rng.standard_normal(idx.size) + 1j * rng.standard_normal(idx.size)
 
     model = cw.model_host[0].astype(numpy.float64)
-    dt, plan, planes, nitems = cpu_gridder_sample(u, v, w, values, model, cw.npixel, cw.cell,
-                                                  cw.epsilon, nplanes_sample, sigma, cores)
-    # scale: all planes, all polarisations (ng.py grids each pol separately)
-    scale = plan.nplanes / len(planes) * cw.npol
+    dt, plan, planes, nitems, t_pol = cpu_gridder_sample(
+        u, v, w, values, model, cw.npixel, cw.cell, cw.epsilon, nplanes_sample, sigma, cores)
+    # scale: all planes and item-planes, all polarisations (ng.py grids each
+    # pol separately)
+    scale = t_pol / dt * cw.npol
     t_full = dt * scale
     mvis = 2 * cw.nvis / t_full / 1e6
     why = ("the fastest on these cores of %s, estimated s per pol: %s"
@@ -526,9 +544,10 @@ def cpu_sample(cw, nplanes_sample):
            if est else "the oversampling choice failed; the default")
     desc = ("oracle C gridder (FP64, OpenMP + scipy.fft pocketfft) at sigma %g, W %d (%s), "
             "invert+predict of one polarisation over %d of %d w-planes (%d items reach them; "
-            "seeded Gaussian values), time scaled by %d/%d planes x %d pols: %.2f s measured"
-            % (sigma, plan.W, why, len(planes), plan.nplanes, nitems, plan.nplanes, len(planes),
-               cw.npol, dt))
+            "seeded Gaussian values), %.2f s measured; the transforms scaled by %d/%d planes, "
+            "the spreading and gathering by all item-planes over the sampled ones, x %d pols"
+            % (sigma, plan.W, why, len(planes), plan.nplanes, nitems, dt, plan.nplanes,
+               len(planes), cw.npol))
     return {"mvis": mvis, "cores": cores, "desc": desc, "sample_s": dt, "full_s": t_full,
             "scale": scale, "sigma": sigma, "W": plan.W, "planes": len(planes),
             "nplanes": plan.nplanes}
@@ -1204,10 +1223,9 @@ def bench_autograd(args):
     s_ = freq / 299792458.0
     uu, vv, ww = [(fun[:, i:i + 1] * s_).ravel() for i in range(3)]
     rng2 = numpy.random.default_rng(2)
-    dt, cplan, planes, nitems = cpu_gridder_sample(
+    dt, cplan, planes, nitems, t_cpu = cpu_gridder_sample(
         uu, vv, ww, lambda idx: rng2.standard_normal(idx.size) + 1j * rng2.standard_normal(
             idx.size), sky, npix, cell, eps, args.cpu_planes, 2.0, cores)
-    t_cpu = dt * cplan.nplanes / len(planes)
     plan.close()
     workload = {"workload": "differentiable predict: %d^2 FP32 sky (200 points + 20 Gaussian "
                             "blobs), %d antennas (%d baselines) x %d times, %d chan %.0f-%.0f "

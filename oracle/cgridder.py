@@ -14,6 +14,7 @@ an evenly spread subset as a bounded sample and scales the time by
 import ctypes
 import os
 import subprocess
+import time
 
 import numpy
 import scipy.fft
@@ -122,8 +123,19 @@ class Prepared:
         return idx, numpy.ascontiguousarray(starts)
 
 
-def grid_items(pr, c, nthreads=None, planes=None):
-    """Dirty image [ny][nx] from item values c (weights applied), FP64."""
+def _tick(timing, key, t0, n=0):
+    """Add the seconds since t0 (and n item-planes) to timing[key]."""
+    if timing is not None:
+        timing[key] = timing.get(key, 0.0) + time.perf_counter() - t0
+        timing["item_planes"] = timing.get("item_planes", 0) + n
+    return time.perf_counter()
+
+
+def grid_items(pr, c, nthreads=None, planes=None, timing=None):
+    """Dirty image [ny][nx] from item values c (weights applied), FP64.
+    ``timing`` (a dict), when given, accumulates the seconds spent on the
+    items' spreading ("items") and on the per-plane transforms and screens
+    ("planes"), and the item-planes spread ("item_planes")."""
     lib = _load()
     nthreads = nthreads or max_threads()
     pl = pr.plan
@@ -136,22 +148,26 @@ def grid_items(pr, c, nthreads=None, planes=None):
         idx = pr.items_of_plane(k)
         if idx.size == 0:
             continue
+        t0 = time.perf_counter()
         order, starts = pr.banded(idx)
         grid[...] = 0
         lib.og_grid_plane(pl.ngx, pl.ngy, pl.W, pl.beta, int(pl.do_w), int(k), _p(pr.p0),
                           _p(pr.q0), _p(pr.k0), _p(pr.du), _p(pr.dv), _p(pr.dwf), _p(cv),
                           _p(order), _p(starts), int(pr.nbands), _p(grid.view(numpy.float64)),
                           nthreads)
+        t0 = _tick(timing, "items", t0, idx.size)
         img = scipy.fft.ifft2(grid, norm="forward", workers=nthreads, overwrite_x=True)
         img = numpy.ascontiguousarray(img)
         lib.og_screen_acc(pl.nx, pl.ny, pl.ngx, pl.ngy, int(pl.do_w), float(pl.w_plane(k)),
                           None if pr.tprime is None else _p(pr.tprime),
                           _p(img.view(numpy.float64)), _p(acc), nthreads)
+        _tick(timing, "planes", t0)
     return acc * pr.corr
 
 
-def degrid_items(pr, image_yx, nthreads=None, planes=None):
-    """Item values from a real image [ny][nx], FP64."""
+def degrid_items(pr, image_yx, nthreads=None, planes=None, timing=None):
+    """Item values from a real image [ny][nx], FP64 (``timing`` as in
+    :func:`grid_items`)."""
     lib = _load()
     nthreads = nthreads or max_threads()
     pl = pr.plan
@@ -163,14 +179,17 @@ def degrid_items(pr, image_yx, nthreads=None, planes=None):
         idx = pr.items_of_plane(k)
         if idx.size == 0:
             continue
+        t0 = time.perf_counter()
         lib.og_screen_pad(pl.nx, pl.ny, pl.ngx, pl.ngy, int(pl.do_w), float(pl.w_plane(k)),
                           None if pr.tprime is None else _p(pr.tprime), _p(img),
                           _p(grid.view(numpy.float64)), nthreads)
         g = numpy.ascontiguousarray(scipy.fft.fft2(grid, workers=nthreads))
+        t0 = _tick(timing, "planes", t0)
         idx = numpy.ascontiguousarray(idx, dtype=numpy.int64)
         lib.og_degrid_plane(pl.ngx, pl.ngy, pl.W, pl.beta, int(pl.do_w), int(k), _p(pr.p0),
                             _p(pr.q0), _p(pr.k0), _p(pr.du), _p(pr.dv), _p(pr.dwf), _p(idx),
                             int(idx.size), _p(g.view(numpy.float64)), _p(ov), nthreads)
+        _tick(timing, "items", t0, idx.size)
     out = out * numpy.conj(pr.ph)
     return numpy.where(pr.flip, numpy.conj(out), out)
 

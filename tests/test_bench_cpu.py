@@ -36,9 +36,10 @@ def test_sampled_gridding_covers_the_items_reaching_the_planes():
         seen["idx"] = idx
         return numpy.ones(idx.size, numpy.complex128)
 
-    dt, plan, planes, n = bench.cpu_gridder_sample(u, v, w, values, numpy.zeros((64, 64)), 64,
-                                                   4e-3, 1e-5, 3, 1.5, 2)
+    dt, plan, planes, n, est = bench.cpu_gridder_sample(u, v, w, values, numpy.zeros((64, 64)),
+                                                        64, 4e-3, 1e-5, 3, 1.5, 2)
     assert dt > 0 and plan.sigma == 1.5 and len(planes) == 3 and n == seen["idx"].size
+    assert est > dt  # the whole run holds more planes and item-planes than the sample
     ref = owg.Plan(64, 64, 4e-3, 4e-3, 1e-5, True, *owg.w_range(w, True), 1.5)
     a = numpy.ceil((numpy.abs(w) - ref.w_lo) / ref.dw)  # w < 0 items are mirrored
     reach = [i for i in range(w.size) if any(k - ref.W + 1 <= a[i] <= k for k in planes)]
