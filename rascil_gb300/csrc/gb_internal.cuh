@@ -30,6 +30,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kChunkItems = 256;                // items per work chunk
 constexpr int kMaxSupport = 16;
 constexpr int kMaxQuad = 48;                    // Gauss-Legendre nodes (half interval)
+constexpr int kMaxSlab = 128;                   // w-planes per bucket slab
 
 struct Geom {
   int nx, ny;        // image

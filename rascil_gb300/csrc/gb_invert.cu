@@ -129,6 +129,16 @@ __device__ __forceinline__ void grid_add(double2 *dst, double re, double im) {
   atomicAdd(&dst->x, re);
   atomicAdd(&dst->y, im);
 }
+// Two adjacent cells (dst 16-byte aligned): one vector atomic in FP32.
+__device__ __forceinline__ void grid_add2(float2 *dst, float re0, float im0, float re1,
+                                          float im1) {
+  atomicAdd(reinterpret_cast<float4 *>(dst), make_float4(re0, im0, re1, im1));
+}
+__device__ __forceinline__ void grid_add2(double2 *dst, double re0, double im0, double re1,
+                                          double im1) {
+  grid_add(dst, re0, im0);
+  grid_add(dst + 1, re1, im1);
+}
 
 // Slab range [s_lo, s_hi] whose items reach planes [b0, b0 + nb).
 __device__ __forceinline__ void batch_slabs(const Geom &g, int b0, int nb, int &s_lo,
@@ -173,14 +183,15 @@ template <> struct GridSmem<double> {
 // bucket) into the planes [b0, b0 + nb) of `grid`: spread every item over
 // its W x W support in the shared sub-grid, plane by plane, then flush the
 // sub-grid to HBM with float2 atomics and leave it zeroed.  `acc` must be all
-// zero on entry (it is on exit); kc / cc are the FP32 item cache; s_red and
-// s_scale are block-shared scratch.  Every thread of the block calls it.
+// zero on entry (it is on exit); kc / cc are the FP32 item cache; s_red,
+// s_scale and s_first (kMaxSlab + 1 entries) are block-shared scratch.
+// Every thread of the block calls it.
 template <typename R, int NP, int AW>
 __device__ __forceinline__ void grid_chunk(
     const Geom &g, const typename Traits<R>::Item *__restrict__ items,
     const typename Traits<R>::C *__restrict__ cvis, const Chunk ch, int b0, int nb,
     typename Traits<R>::C *__restrict__ grid, typename FixedAcc<R>::T *acc, R *kc,
-    typename Traits<R>::C *cc, double *s_red, R *s_scale) {
+    typename Traits<R>::C *cc, double *s_red, R *s_scale, int *s_first) {
   using C = typename Traits<R>::C;
   using A = typename FixedAcc<R>::T;
   using LM = LaneMap<NP, AW>;
@@ -200,8 +211,13 @@ __device__ __forceinline__ void grid_chunk(
     const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
     const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
     const int kbase = slab * g.S;
-    const int k_lo = max(kbase, b0);
-    const int k_hi = min(min(kbase + g.S + W - 1, g.nplanes), b0 + nb);
+    // a chunk's items run in order of first w-plane (sort_key): its planes
+    // span from its first item's first plane to its last item's last
+    const int lk_first = (int)((items[ch.begin].loc >> 16) & 0xffu);
+    const int lk_last = (int)((items[ch.end - 1].loc >> 16) & 0xffu);
+    const int k_lo = max(kbase + lk_first, b0);
+    const int k_hi = min(min(kbase + lk_last + W, g.nplanes), b0 + nb);
+    if (k_lo >= k_hi) return;  // (block-uniform) no item reaches this batch's planes
     const int n = (int)(ch.end - ch.begin);
     const bool direct = n * W * W < SW2;
     // chunk scale for the fixed-point sub-grid: 2^k / sum_j max |component|
@@ -233,6 +249,17 @@ __device__ __forceinline__ void grid_chunk(
       inv = s_scale[1];
     }
     __syncthreads();  // s_red, s_scale and s_ci are reused by the next chunk
+    // A bucket's items run in order of first w-plane inside the slab (lk):
+    // s_first[l] = the first item of the chunk with lk >= l, so the items
+    // reaching plane k (lk in [k - kbase - W + 1, k - kbase]) are one run.
+    for (int jj = threadIdx.x; jj < n; jj += kThreads) {
+      const int lk = (int)((items[ch.begin + jj].loc >> 16) & 0xffu);
+      const int lkp = jj == 0 ? -1 : (int)((items[ch.begin + jj - 1].loc >> 16) & 0xffu);
+      for (int q = lkp + 1; q <= lk; ++q) s_first[q] = jj;
+      if (jj == n - 1)
+        for (int q = lk + 1; q <= g.S; ++q) s_first[q] = n;
+    }
+    if constexpr (!kCache) __syncthreads();
     if constexpr (kCache) {
       const R f = direct ? (R)1 : scale;
       for (int jj = threadIdx.x; jj < n; jj += kThreads) {
@@ -256,7 +283,10 @@ __device__ __forceinline__ void grid_chunk(
     }
     for (int k = k_lo; k < k_hi; ++k) {
       C *gplane = grid + (size_t)(k - b0) * NP * plane;
-      for (uint32_t j = ch.begin + warp; j < ch.end; j += kWarps) {
+      const int lk_lo = max(0, k - kbase - W + 1), lk_hi = min(g.S - 1, k - kbase);
+      const uint32_t j_lo = ch.begin + (uint32_t)s_first[lk_lo];
+      const uint32_t j_hi = lk_lo <= lk_hi ? ch.begin + (uint32_t)s_first[lk_hi + 1] : j_lo;
+      for (uint32_t j = j_lo + warp; j < j_hi; j += kWarps) {
         const int jj = (int)(j - ch.begin);
         R fw, ku, kv_lane = (R)0;
         uint32_t loc;
@@ -335,22 +365,32 @@ __device__ __forceinline__ void grid_chunk(
       }
       if (!direct) {
         __syncthreads();
-        // flush: fixed point -> float, add to HBM, and leave the sub-grid zeroed
-        for (int i = threadIdx.x; i < SW2; i += kThreads) {
-          const int y = i / SW, x = i - y * SW;
+        // flush: fixed point -> float, add to HBM, and leave the sub-grid
+        // zeroed.  A thread takes two adjacent cells (x even): one 16-byte
+        // vector atomic per pol for both (tile origins, x and the grid width
+        // are even, so p is even and the pair never straddles the wrap).  For
+        // odd SW the last pair's second cell is row padding, never written,
+        // so it adds zero.
+        const int hp = (SW + 1) >> 1;  // cell pairs per sub-grid row
+        for (int i = threadIdx.x; i < SW * hp; i += kThreads) {
+          const int y = i / hp, x = 2 * (i - y * hp);
           const int cell = y * L.pitch + x;
           int p = tu * T + x;
           while (p >= g.ngx) p -= g.ngx;
           int q = tv * T + y;
           while (q >= g.ngy) q -= g.ngy;
-          const R sgn = ((p + q) & 1) ? -inv : inv;
+          const R sgn = ((p + q) & 1) ? -inv : inv;  // the pair's second cell: -sgn
 #pragma unroll
           for (int pol = 0; pol < NP; ++pol) {
-            const A re = acc[pol * L.plane + cell], im = acc[(NP + pol) * L.plane + cell];
-            if (re != 0 || im != 0) {
-              acc[pol * L.plane + cell] = 0;
-              acc[(NP + pol) * L.plane + cell] = 0;
-              grid_add(&gplane[pol * plane + (size_t)q * g.ngx + p], sgn * (R)re, sgn * (R)im);
+            A *are = acc + pol * L.plane + cell, *aim = acc + (NP + pol) * L.plane + cell;
+            const A re0 = are[0], re1 = are[1], im0 = aim[0], im1 = aim[1];
+            if ((re0 | re1 | im0 | im1) != 0) {
+              are[0] = 0;
+              are[1] = 0;
+              aim[0] = 0;
+              aim[1] = 0;
+              grid_add2(&gplane[pol * plane + (size_t)q * g.ngx + p], sgn * (R)re0,
+                        sgn * (R)im0, -sgn * (R)re1, -sgn * (R)im1);
             }
           }
         }
@@ -382,12 +422,14 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t s_ci;
   __shared__ double s_red[kWarps];
   __shared__ R s_scale[2];
+  __shared__ int s_first[kMaxSlab + 1];
   for (;;) {
     if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
     __syncthreads();
     const uint32_t ci = s_ci;
     if (ci >= c_end) break;
-    grid_chunk<R, NP, AW>(g, items, cvis, chunks[ci], b0, nb, grid, acc, kc, cc, s_red, s_scale);
+    grid_chunk<R, NP, AW>(g, items, cvis, chunks[ci], b0, nb, grid, acc, kc, cc, s_red, s_scale,
+                          s_first);
   }
 }
 
@@ -705,6 +747,7 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ int s_j;
   __shared__ double s_red[kWarps];
   __shared__ float s_scale[2];
+  __shared__ int s_first[kMaxSlab + 1];
   if (threadIdx.x == 0) {
     uint32_t w = 0;
     for (int j = 0; j < jobs.n; ++j) {
@@ -739,7 +782,7 @@ __global__ void __launch_bounds__(kThreads)
     grid_chunk<float, NP, AW>(jb.g, reinterpret_cast<const ItemF *>(jb.items),
                               reinterpret_cast<const float2 *>(jb.cvis), jb.chunks[ci], jb.b0,
                               jb.nb, reinterpret_cast<float2 *>(jb.grid), acc, kc, cc, s_red,
-                              s_scale);
+                              s_scale, s_first);
   }
 }
 

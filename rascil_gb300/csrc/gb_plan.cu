@@ -242,8 +242,8 @@ static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi
     return GB_ERR_INVALID_ARG;
   }
   int S = p->slab > 0 ? p->slab : 4;
-  if (S > 128) {
-    set_error("slab %d outside [1, 128]", S);
+  if (S > kMaxSlab) {
+    set_error("slab %d outside [1, %d]", S, kMaxSlab);
     return GB_ERR_INVALID_ARG;
   }
   g.T = T;
@@ -252,8 +252,10 @@ static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi
   g.ntv = (g.ngy + T - 1) / T;
   g.nslabs = (g.nplanes + S - 1) / S;
   g.nbuckets = (int64_t)g.nslabs * g.ntu * g.ntv;
-  if (g.nbuckets >= (int64_t)0xffffffffLL) {
-    set_error("too many buckets (%lld)", (long long)g.nbuckets);
+  // the sort keys order items by bucket, then by first w-plane inside the
+  // slab: nbuckets x S keys
+  if (g.nbuckets * S >= (int64_t)0xffffffffLL) {
+    set_error("too many buckets (%lld x %d w-planes per slab)", (long long)g.nbuckets, S);
     return GB_ERR_INVALID_ARG;
   }
   const int64_t nitems = p->nrows * (int64_t)p->nchan;
@@ -417,6 +419,14 @@ __global__ void k_wrange(const double *__restrict__ uvw, int64_t nrows, int mirr
 // ---------------------------------------------------------------------
 // Bucket sort
 
+// Sort key of an item: its bucket, then its first w-plane inside the slab,
+// so a bucket's items run in order of first w-plane (the kernels then find
+// the items reaching one w-plane as one contiguous run, and the lanes of a
+// warp reach the same w-planes).
+__host__ __device__ inline uint32_t sort_key(const Geom &g, const Coord &o) {
+  return bucket_of(g, o) * (uint32_t)g.S + (uint32_t)(o.k0 % g.S);
+}
+
 __global__ void k_count(const Geom g, const double *__restrict__ uvw,
                         const double *__restrict__ freq, uint32_t *__restrict__ counts,
                         uint32_t *__restrict__ keys, uint32_t *__restrict__ ranks) {
@@ -429,7 +439,7 @@ __global__ void k_count(const Geom g, const double *__restrict__ uvw,
     if (active) {
       Coord o;
       item_coord(g, uvw, freq, (uint32_t)i, o);
-      key = bucket_of(g, o);
+      key = sort_key(g, o);
     }
     // warp-aggregated increment: one atomic per distinct key in the warp
     const uint32_t peers = __match_any_sync(0xffffffffu, key);
@@ -481,21 +491,23 @@ __global__ void k_scatter(const Geom g, const double *__restrict__ uvw,
   }
 }
 
-__global__ void k_chunk_counts(const uint32_t *__restrict__ offsets, int64_t nbuckets,
+// offsets[] is over sort keys (S per bucket): bucket b's items are
+// [offsets[b S], offsets[(b + 1) S]).
+__global__ void k_chunk_counts(const uint32_t *__restrict__ offsets, int S, int64_t nbuckets,
                                uint32_t *__restrict__ ccounts) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbuckets; b += stride) {
-    const uint32_t n = offsets[b + 1] - offsets[b];
+    const uint32_t n = offsets[(b + 1) * S] - offsets[b * S];
     ccounts[b] = (n + kChunkItems - 1) / kChunkItems;
   }
 }
 
-__global__ void k_emit_chunks(const uint32_t *__restrict__ offsets,
+__global__ void k_emit_chunks(const uint32_t *__restrict__ offsets, int S,
                               const uint32_t *__restrict__ chunk_off, int64_t nbuckets,
                               Chunk *__restrict__ chunks) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbuckets; b += stride) {
-    const uint32_t lo = offsets[b], hi = offsets[b + 1];
+    const uint32_t lo = offsets[b * S], hi = offsets[(b + 1) * S];
     uint32_t c = chunk_off[b];
     for (uint32_t s = lo; s < hi; s += kChunkItems, ++c) {
       Chunk ch;
@@ -509,9 +521,9 @@ __global__ void k_emit_chunks(const uint32_t *__restrict__ offsets,
 }
 
 __global__ void k_slab_items(const uint32_t *__restrict__ offsets, int nslabs, int64_t ntiles,
-                             uint32_t *__restrict__ out) {
+                             int S, uint32_t *__restrict__ out) {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s <= nslabs; s += gridDim.x * blockDim.x)
-    out[s] = offsets[(int64_t)s * ntiles];
+    out[s] = offsets[(int64_t)s * ntiles * S];
 }
 
 // Correction image [ny][nx]: 1/(phihat_u phihat_v) and, with w-stacking,
@@ -848,14 +860,15 @@ static int layout_workspace(gb_plan *p) {
   t = align_up(t + 4 * (size_t)g.nitems);
   p->t_ranks = t;
   t = align_up(t + 4 * (size_t)g.nitems);
+  const int64_t nk1 = g.nbuckets * g.S + 1;  // sort keys (+ the end)
   p->t_counts = t;
-  t = align_up(t + 4 * (size_t)nb1);
+  t = align_up(t + 4 * (size_t)nk1);
   p->t_offsets = t;
-  t = align_up(t + 4 * (size_t)nb1);
+  t = align_up(t + 4 * (size_t)nk1);
   p->t_ccounts = t;
   t = align_up(t + 4 * (size_t)nb1);
   p->t_scan = t;
-  t = align_up(t + 4 * scan_tmp_words(nb1));
+  t = align_up(t + 4 * scan_tmp_words(nk1));
   const size_t bind_temp = t;
   // call temporaries
   size_t c = 0;
@@ -891,7 +904,8 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   const unsigned bucket_blocks = (unsigned)std::min<int64_t>(
       (nb + kThreads - 1) / kThreads, (int64_t)p->num_sms * 16);
   const double ni = (double)g.nitems, rows = (double)g.R * 24.0 + 8.0 * g.C;
-  GB_CUDA(cudaMemsetAsync(counts, 0, 4 * (size_t)(nb + 1), s));
+  const int64_t nk = nb * g.S;  // sort keys
+  GB_CUDA(cudaMemsetAsync(counts, 0, 4 * (size_t)(nk + 1), s));
   GB_CUDA(cudaMemsetAsync(p->status_word(), 0, 4, s));
   if (g.shifted) {
     GB_CUDA(cudaMemcpyAsync(p->at<double>(p->off_coords), p->uvw, 24 * (size_t)g.R,
@@ -906,8 +920,8 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   }
   int rc;
   {
-    ProfScope ps(kProfScan, s, 8.0 * (double)(nb + 1));
-    rc = scan_exclusive(counts, offsets, nb, stmp, s);
+    ProfScope ps(kProfScan, s, 8.0 * (double)(nk + 1));
+    rc = scan_exclusive(counts, offsets, nk, stmp, s);
   }
   if (rc) return rc;
   {
@@ -918,18 +932,19 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   }
   {
     ProfScope ps(kProfChunks, s, 20.0 * (double)(nb + 1) + 16.0 * ni / kChunkItems);
-    k_chunk_counts<<<bucket_blocks, kThreads, 0, s>>>(offsets, nb, ccounts);
+    k_chunk_counts<<<bucket_blocks, kThreads, 0, s>>>(offsets, g.S, nb, ccounts);
     GB_LAUNCH_CHECK("k_chunk_counts");
     rc = scan_exclusive(ccounts, chunk_off, nb, stmp, s);
     if (rc) return rc;
-    k_emit_chunks<<<bucket_blocks, kThreads, 0, s>>>(offsets, chunk_off, nb, chunks);
+    k_emit_chunks<<<bucket_blocks, kThreads, 0, s>>>(offsets, g.S, chunk_off, nb, chunks);
     GB_LAUNCH_CHECK("k_emit_chunks");
   }
   // first item of every slab, to the host: only the profiler's byte counts
   // use it, and it costs a synchronisation, so only while profiling is on
   if (prof_on()) {
     uint32_t *slab_dev = ccounts;  // reuse: ccounts is free after the chunk scan
-    k_slab_items<<<4, kThreads, 0, s>>>(offsets, g.nslabs, (int64_t)g.ntu * g.ntv, slab_dev);
+    k_slab_items<<<4, kThreads, 0, s>>>(offsets, g.nslabs, (int64_t)g.ntu * g.ntv, g.S,
+                                        slab_dev);
     GB_LAUNCH_CHECK("k_slab_items");
     p->slab_items.assign((size_t)g.nslabs + 1, 0u);
     GB_CUDA(cudaMemcpyAsync(p->slab_items.data(), slab_dev, 4 * ((size_t)g.nslabs + 1),

@@ -149,8 +149,12 @@ __global__ void __launch_bounds__(kThreads)
     const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
     const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
     const int kbase = slab * g.S;
-    const int k_lo = max(kbase, b0);
-    const int k_hi = min(min(kbase + g.S + W - 1, g.nplanes), b0 + nb);
+    // a chunk's items run in order of first w-plane (sort_key): its planes
+    // span from its first item's first plane to its last item's last
+    const int lk_first = (int)((items[ch.begin].loc >> 16) & 0xffu);
+    const int lk_last = (int)((items[ch.end - 1].loc >> 16) & 0xffu);
+    const int k_lo = max(kbase + lk_first, b0);
+    const int k_hi = min(min(kbase + lk_last + W, g.nplanes), b0 + nb);
     const int n = (int)(ch.end - ch.begin);
     const bool direct = n * W * W < SW2;
     R ar[NP], ai[NP];  // lane i: running sums of item warp*32 + i
@@ -362,8 +366,13 @@ __device__ __forceinline__ void degrid_lane_chunk(
     const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
     const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
     const int kbase = slab * g.S;
-    const int k_lo = max(kbase, b0);
-    const int k_hi = min(min(kbase + g.S + WT - 1, g.nplanes), b0 + nb);
+    // a chunk's items run in order of first w-plane (sort_key): its planes
+    // span from its first item's first plane to its last item's last
+    const int lk_first = (int)((items[ch.begin].loc >> 16) & 0xffu);
+    const int lk_last = (int)((items[ch.end - 1].loc >> 16) & 0xffu);
+    const int k_lo = max(kbase + lk_first, b0);
+    const int k_hi = min(min(kbase + lk_last + WT, g.nplanes), b0 + nb);
+    if (k_lo >= k_hi) return;  // (block-uniform) no item reaches this batch's planes
     const int n = (int)(ch.end - ch.begin);
     const bool direct = n * WT * WT < SW * SW;
     const bool has = (int)threadIdx.x < n;
