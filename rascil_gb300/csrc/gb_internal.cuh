@@ -31,6 +31,8 @@ constexpr int kChunkItems = 256;                // items per work chunk
 constexpr int kMaxSupport = 16;
 constexpr int kMaxQuad = 48;                    // Gauss-Legendre nodes (half interval)
 constexpr int kMaxSlab = 128;                   // w-planes per bucket slab
+constexpr int kMaxTile = 128;                   // uv tile side (cells)
+constexpr int kMaxSubSide = kMaxTile + kMaxSupport - 1;  // tile plus support halo
 
 struct Geom {
   int nx, ny;        // image
@@ -327,6 +329,11 @@ inline __host__ __device__ int congruent_up(int x, int m) {
 }
 
 inline __host__ __device__ int group_lanes(int W) { return W <= 8 ? 8 : 16; }
+
+// Floats per item in the FP32 gridder's shared-memory item cache: the
+// packed location word (padded to 16 bytes), then the u, v and w kernel
+// values, AW each (zero beyond W), so every group starts on 16 bytes.
+inline __host__ __device__ constexpr int kcache_stride(int AW) { return 4 + 3 * AW; }
 
 struct TileLayout {
   int SW, pitch, plane;

@@ -179,6 +179,81 @@ template <> struct GridSmem<double> {
   static constexpr bool kCache = false;
 };
 
+// The FP32 gridder's spread of the items reaching plane k (chunk-relative
+// [jj_lo, jj_hi), all with their w-support on k) into the fixed-point
+// sub-grid: two items per warp iteration (independent chains of atomics),
+// kernel values from the item cache -- a lane's u value folded into its
+// values once, the v values of every support row by 16-byte broadcast
+// loads -- then per support row and part one multiply, one conversion and
+// one shared atomic.
+template <int NP, int AW>
+__device__ __forceinline__ void spread_fixed(const LaneMap<NP, AW> &lm, int warp, int W, int k,
+                                             int kbase, int jj_lo, int jj_hi,
+                                             const float *__restrict__ kc,
+                                             const float2 *__restrict__ cc, int *acc,
+                                             const TileLayout &L) {
+  using LM = LaneMap<NP, AW>;
+  constexpr int KS = kcache_stride(AW);
+  constexpr int kMaxRows = (AW + LM::RS - 1) / LM::RS;
+  const bool lane_in = lm.a < W;
+  for (int j0 = jj_lo + warp; j0 < jj_hi; j0 += 2 * kWarps) {
+    const bool two = j0 + kWarps < jj_hi;  // warp-uniform
+    float kv[2][LM::RS == 1 ? AW : 1];
+    float2 c[2][LM::NPL];
+    int cell0[2];
+    const float *kjs[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int jj = (u == 1 && two) ? j0 + kWarps : j0;
+      const float *kj = kc + jj * KS;
+      kjs[u] = kj;
+      const uint32_t loc = __float_as_uint(kj[0]);
+      const int aw = k - (kbase + (int)((loc >> 16) & 0xffu));  // in [0, W) here
+      const float f = kj[4 + 2 * AW + aw] * kj[4 + lm.a];        // kw(aw) ku(a)
+      if constexpr (LM::RS == 1) {
+#pragma unroll
+        for (int q = 0; q < AW; q += 4) {
+          const float4 t = *reinterpret_cast<const float4 *>(kj + 4 + AW + q);
+          kv[u][q] = t.x;
+          kv[u][q + 1] = t.y;
+          kv[u][q + 2] = t.z;
+          kv[u][q + 3] = t.w;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < LM::NPL; ++i) {
+        const float2 v = cc[jj * NP + lm.pol(i)];
+        c[u][i] = make_float2(v.x * f, v.y * f);
+      }
+      const int lu = (int)(loc & 0xffu), lv = (int)((loc >> 8) & 0xffu);
+      cell0[u] = (lv + lm.r0) * L.pitch + lu + lm.a;
+    }
+#pragma unroll
+    for (int r = 0; r < kMaxRows; ++r) {
+      if (LM::RS == 1 && r >= W) break;  // warp-uniform
+      const int b = lm.r0 + r * LM::RS;
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (u == 1 && !two) break;  // warp-uniform
+        if (b < W && lane_in) {
+          float kvb;
+          if constexpr (LM::RS == 1)
+            kvb = kv[u][r];
+          else
+            kvb = kjs[u][4 + AW + b];
+          const int cell = cell0[u] + r * LM::RS * L.pitch;
+#pragma unroll
+          for (int i = 0; i < LM::NPL; ++i) {
+            const int pl = lm.pol(i);
+            fixed_add(&acc[pl * L.plane + cell], to_fixed(kvb * c[u][i].x));
+            fixed_add(&acc[(NP + pl) * L.plane + cell], to_fixed(kvb * c[u][i].y));
+          }
+        }
+      }
+    }
+  }
+}
+
 // Grid one work chunk (up to kChunkItems items of one (w-slab, uv tile)
 // bucket) into the planes [b0, b0 + nb) of `grid`: spread every item over
 // its W x W support in the shared sub-grid, plane by plane, then flush the
@@ -198,7 +273,7 @@ __device__ __forceinline__ void grid_chunk(
   constexpr bool kCache = GridSmem<R>::kCache;
   const int W = g.W, T = g.T;
   const TileLayout L = tile_layout(T, W, NP);
-  const int KS = 3 * W + 1;
+  constexpr int KS = kcache_stride(AW);  // item cache: loc | ku[AW] | kv[AW] | kw[AW]
   const int SW = L.SW, SW2 = SW * SW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const LM lm(lane);
@@ -266,10 +341,13 @@ __device__ __forceinline__ void grid_chunk(
         const auto it = items[ch.begin + jj];
         R *c = kc + jj * KS;
         c[0] = __uint_as_float(it.loc);
-        for (int a = 0; a < W; ++a) {
-          c[1 + a] = es_kernel(((R)a - it.du) * scale_u, beta);
-          c[1 + W + a] = es_kernel(((R)a - it.dv) * scale_u, beta);
-          c[1 + 2 * W + a] = g.do_w ? es_kernel(((R)a - it.dwf) * scale_u, beta) : (R)1;
+#pragma unroll
+        for (int a = 0; a < AW; ++a) {
+          const bool in = a < W;
+          c[4 + a] = in ? es_kernel(((R)a - it.du) * scale_u, beta) : (R)0;
+          c[4 + AW + a] = in ? es_kernel(((R)a - it.dv) * scale_u, beta) : (R)0;
+          c[4 + 2 * AW + a] = in ? (g.do_w ? es_kernel(((R)a - it.dwf) * scale_u, beta) : (R)1)
+                                 : (R)0;
         }
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
@@ -286,7 +364,12 @@ __device__ __forceinline__ void grid_chunk(
       const int lk_lo = max(0, k - kbase - W + 1), lk_hi = min(g.S - 1, k - kbase);
       const uint32_t j_lo = ch.begin + (uint32_t)s_first[lk_lo];
       const uint32_t j_hi = lk_lo <= lk_hi ? ch.begin + (uint32_t)s_first[lk_hi + 1] : j_lo;
-      for (uint32_t j = j_lo + warp; j < j_hi; j += kWarps) {
+      if constexpr (kCache) {
+        if (!direct)
+          spread_fixed<NP, AW>(lm, warp, W, k, kbase, (int)(j_lo - ch.begin),
+                               (int)(j_hi - ch.begin), kc, cc, acc, L);
+      }
+      for (uint32_t j = j_lo + warp; j < j_hi && (!kCache || direct); j += kWarps) {
         const int jj = (int)(j - ch.begin);
         R fw, ku, kv_lane = (R)0;
         uint32_t loc;
@@ -296,9 +379,9 @@ __device__ __forceinline__ void grid_chunk(
           loc = __float_as_uint(kj[0]);
           const int aw = k - (kbase + (int)((loc >> 16) & 0xffu));
           if (aw < 0 || aw >= W) continue;
-          fw = kj[1 + 2 * W + aw];
-          ku = lm.a < W ? kj[1 + lm.a] : (R)0;
-          if (lane >= 16 && lane - 16 < W) kv_lane = kj[1 + W + lane - 16];
+          fw = kj[4 + 2 * AW + aw];
+          ku = kj[4 + lm.a];  // zero for a >= W
+          if (lane >= 16 && lane - 16 < W) kv_lane = kj[4 + AW + lane - 16];
 #pragma unroll
           for (int i = 0; i < LM::NPL; ++i) {
             c[i] = cc[jj * NP + lm.pol(i)];
@@ -411,8 +494,8 @@ __global__ void __launch_bounds__(kThreads)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   A *acc = reinterpret_cast<A *>(smem_raw);  // [re pols | im pols][SW][pitch]
   const TileLayout L = tile_layout(g.T, g.W, NP);
-  R *kc = reinterpret_cast<R *>(acc + 2 * NP * L.plane);     // [kChunkItems][3 W + 1]
-  C *cc = reinterpret_cast<C *>(kc + kChunkItems * (3 * g.W + 1));  // [kChunkItems][NP]
+  R *kc = reinterpret_cast<R *>(acc + 2 * NP * L.plane);  // [kChunkItems][kcache_stride]
+  C *cc = reinterpret_cast<C *>(kc + kChunkItems * kcache_stride(AW));  // [kChunkItems][NP]
   const int ntiles = g.ntu * g.ntv;
   int s_lo, s_hi;
   batch_slabs(g, b0, nb, s_lo, s_hi);
@@ -541,7 +624,8 @@ size_t tile_smem_bytes(const gb_plan *p) {
 size_t grid_smem_bytes(const gb_plan *p) {
   size_t b = tile_smem_bytes(p);
   if (p->precision == GB_FP32)
-    b += (size_t)kChunkItems * ((3 * p->g.W + 1) * sizeof(float) + p->g.NP * sizeof(float2));
+    b += (size_t)kChunkItems *
+         (kcache_stride(group_lanes(p->g.W)) * sizeof(float) + p->g.NP * sizeof(float2));
   return b;
 }
 
@@ -822,7 +906,7 @@ int launch_grid_jobs(const GridJobs &jobs, int num_sms, uint32_t *counter, doubl
     }
     const TileLayout L = tile_layout(g.T, g.W, g.NP);
     acc_words = std::max(acc_words, 2 * NP * L.plane);
-    ks_max = std::max(ks_max, 3 * g.W + 1);
+    ks_max = std::max(ks_max, kcache_stride(AW));
   }
   const size_t smem = (size_t)acc_words * 4 + (size_t)kChunkItems * (ks_max * 4 + NP * 8);
   ProfScope ps(kProfGrid, s, bytes, updates);

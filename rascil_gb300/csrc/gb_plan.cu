@@ -237,8 +237,8 @@ static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi
     g.nplanes = 1;
   }
   int T = p->tile > 0 ? p->tile : (p->precision == GB_FP64 ? 16 : 32);
-  if (T < 4 || T > 128) {
-    set_error("tile %d outside [4, 128]", T);
+  if (T < 4 || T > kMaxTile) {
+    set_error("tile %d outside [4, %d]", T, kMaxTile);
     return GB_ERR_INVALID_ARG;
   }
   int S = p->slab > 0 ? p->slab : 4;

@@ -350,7 +350,7 @@ __device__ __forceinline__ void degrid_lane_chunk(
     const Geom &g, const ItemF *__restrict__ items, const Chunk ch, int b0, int nb,
     const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
     const float *__restrict__ wgt, const PolMat &pm, const RowPerm &rp, float2 *stage,
-    float *skv) {
+    float *skv, int *s_rowoff, int *s_col) {
   constexpr int PP = degrid_pass_pols(NP);
   const int T = g.T;
   const int SW = T + WT - 1, rowf2 = lane_row(PP, SW), pstride = SW * rowf2;
@@ -391,6 +391,22 @@ __device__ __forceinline__ void degrid_lane_chunk(
     float2 acc[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
+    // the sub-grid's grid rows (physical row x ngx, in the row order of the
+    // grid) and columns, wrapped once per chunk for every staged plane
+    if (!direct) {
+      for (int i = threadIdx.x; i < 2 * SW; i += kThreads) {
+        if (i < SW) {
+          int q = tv * T + i;
+          while (q >= g.ngy) q -= g.ngy;
+          s_rowoff[i] = rp.row(q) * g.ngx;
+        } else {
+          int pc = tu * T + (i - SW);
+          while (pc >= g.ngx) pc -= g.ngx;
+          s_col[i - SW] = pc;
+        }
+      }
+      __syncthreads();
+    }
     // the pols in passes of PP: each pass stages its pols' sub-grids only,
     // which halves the staging buffers and the per-thread sums for NP = 4
     // (unrolled: acc stays in registers)
@@ -400,17 +416,12 @@ __device__ __forceinline__ void degrid_lane_chunk(
       // commit group per thread
       auto stage_plane = [&](int k, float2 *dst) {
         const float2 *gp = grid + ((int64_t)(k - b0) * NP + pb) * plane;
+        static_assert(PP <= 2, "one or two pols per staging pass");
         for (int r = warp; r < PP * SW; r += kWarps) {
-          const int pol = r / SW, y = r - pol * SW;
-          int q = tv * T + y;
-          while (q >= g.ngy) q -= g.ngy;
-          const float2 *src = gp + pol * plane + (int64_t)rp.row(q) * g.ngx;
+          const int pol = r >= SW ? 1 : 0, y = r - pol * SW;
+          const float2 *src = gp + pol * plane + s_rowoff[y];
           float2 *d = dst + y * rowf2 + pol;
-          for (int x = lane; x < SW; x += 32) {
-            int pc = tu * T + x;
-            while (pc >= g.ngx) pc -= g.ngx;
-            cp_async8(d + x * PP, src + pc, true);
-          }
+          for (int x = lane; x < SW; x += 32) cp_async8(d + x * PP, src + s_col[x], true);
         }
         cp_async_commit();
       };
@@ -551,6 +562,7 @@ __global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
   const int SW = g.T + WT - 1, pstride = SW * lane_row(degrid_pass_pols(NP), SW);
   float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][rowf2]
   float *skv = reinterpret_cast<float *>(stage + 2 * pstride);   // [WT][kThreads]: own kv
+  __shared__ int s_rowoff[kMaxSubSide], s_col[kMaxSubSide];
   const int ntiles = g.ntu * g.ntv;
   const int lo = b0 - (g.S + WT - 2);
   const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
@@ -565,7 +577,7 @@ __global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
     __syncthreads();  // every thread has read s_ci
     if (ci >= c_end) break;
     degrid_lane_chunk<NP, WT>(g, items, chunks[ci], b0, nb, grid, vis, npv, wgt, pm, rp, stage,
-                              skv);
+                              skv, s_rowoff, s_col);
   }
 }
 
@@ -588,6 +600,7 @@ __global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
   }
   float2 *stage = reinterpret_cast<float2 *>(smem_raw);
   float *skv = reinterpret_cast<float *>(stage + 2 * pstride_max);
+  __shared__ int s_rowoff[kMaxSubSide], s_col[kMaxSubSide];
   if (threadIdx.x == 0) {
     uint32_t w = 0;
     for (int j = 0; j < jobs.n; ++j) {
@@ -625,7 +638,7 @@ __global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
     degrid_lane_chunk<NP, WT>(jb.g, reinterpret_cast<const ItemF *>(jb.items), jb.chunks[ci],
                               jb.b0, jb.nb, reinterpret_cast<const float2 *>(jb.grid),
                               reinterpret_cast<float2 *>(jb.vis), jb.npv, jb.wgt, pm, jb.rp,
-                              stage, skv);
+                              stage, skv, s_rowoff, s_col);
   }
 }
 
