@@ -15,7 +15,7 @@
 //   grid     ONE persistent k_grid_jobs launch per (pols, lane width) grids
 //            every invert job's chunks, fed from a device work queue (the
 //            jobs' chunk ranges concatenated, one atomic counter);
-//   degrid   ONE persistent k_degrid_lane_jobs launch per (pols, support)
+//   degrid   ONE persistent k_degrid_warp_jobs launch per (pols, lane width)
 //            degrids every predict job's chunks the same way;
 //   fork     each invert job's transforms, screens and image accumulation
 //            (and its plan's correction pass after the last batch) run on

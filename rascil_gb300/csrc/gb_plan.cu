@@ -67,7 +67,7 @@ static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi
 // plus per-plane transform work per grid cell and polarisation -- the
 // library's pruned row/column transforms where they apply, batched 2-D
 // cuFFT plans with separate zeroing and screen passes otherwise.  Constants
-// measured on the LOW-like workload (k_grid / k_degrid_lane per update; the
+// measured on the LOW-like workload (k_grid / k_degrid_warp per update; the
 // column-mode passes and cuFFT planes per cell).
 constexpr double kCostItemPlane[2] = {9.3e-11, 2.5e-9};  // FP32, FP64 (at W = 7)
 constexpr double kCostCellColumns = 4.7e-12;

@@ -7,16 +7,18 @@
 //                           image * exp(+2 pi i w_k (n-1-tc)), the rest 0
 //                           (no separate memset pass).
 //             cuFFT         2-D c2c, e^{-2 pi i}
-//             k_degrid      one CTA per work chunk: the tile's sub-grid of
-//                           each plane is staged in shared memory from
-//                           coalesced 16-byte grid rows; each warp walks its
-//                           items, each lane sums a slice of the W x W
-//                           support and the partial sums are reduced with
-//                           warp shuffles; lane i keeps item i's running
-//                           sum over planes.  The epilogue rotates back by
-//                           exp(+2 pi i w tc), applies the pol-frame matrix
-//                           and weights and writes (first batch of the
-//                           item) or accumulates (later batches) in place.
+//             k_degrid_warp one CTA per work chunk (FP32 form): every item's
+//                           kernel values cached once per chunk; per plane a
+//                           warp per item reads its W x W support straight
+//                           from the grid (a lane group's eight lanes read
+//                           one 64-byte row segment), weights it and sums
+//                           the lanes with shuffles into the item's running
+//                           sums.  k_degrid (FP64 form) stages each plane's
+//                           sub-grid in shared memory instead.  The
+//                           epilogue rotates back by exp(+2 pi i w tc),
+//                           conjugates mirrored items, applies the pol-frame
+//                           matrix and weights and writes (first batch of
+//                           the item) or accumulates (later batches) in place.
 #include <cufft.h>
 
 #include "gb_async.cuh"
@@ -318,296 +320,298 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// float2 elements from one staged row to the next in k_degrid_lane: SW
-// cells padded to an odd count, plus one 16-byte unit for NP = 4.
-__host__ __device__ constexpr int lane_row(int NP, int SW) {
-  return (SW | 1) * NP + (NP == 4 ? 2 : 0);
-}
-
-// Pols summed per staging pass of k_degrid_lane: two for NP = 4 (half the
-// staging and per-thread sums, so more CTAs fit an SM), else all.
-__host__ __device__ constexpr int degrid_pass_pols(int NP) { return NP == 4 ? 2 : NP; }
-
-// FP32 degridder, one item per thread.  A CTA takes a chunk (up to 256
-// items of one bucket); thread i owns item i: its u and v kernel values
-// (with the checkerboard sign (-1)^(p+q) folded in) stay in registers for
-// all planes, and for every plane the thread sums its whole W x W footprint
-// from the plane's staged sub-grid ([SW][pitch][NP] complex, a cell's pols
-// contiguous), double-buffered with cp.async so plane k + 1 streams in
-// while plane k is summed.  Staged rows are lane_row(NP, SW) float2 apart:
-// an odd number of 16-byte units for NP = 4 (whose cells are two 16-byte
-// units), so one load instruction's 32 cells spread over all eight 16-byte
-// bank groups instead of the four of one parity.
-// Per item-plane that is W^2 NP shared loads and 2 W^2 NP FMAs with no
-// cross-lane reduction, against the warp-per-item map of k_degrid.
-// Degrid one work chunk (up to kChunkItems items of one bucket, thread i
-// owning item i) over the planes [b0, b0 + nb) of `grid` into vis.  stage /
-// skv: the block's shared staging buffers (2 x [SW][rowf2] float2, then
-// [WT][kThreads] floats).  Every thread of the block calls it; it ends with
-// the staging buffers free.
-template <int NP, int WT>
-__device__ __forceinline__ void degrid_lane_chunk(
+// FP32 degridder, warp per item, reading the grid directly (no staging
+// pass).  A CTA takes a work chunk (up to kChunkItems items of one (w-slab,
+// uv tile) bucket).  Once per chunk it caches in shared memory every item's
+// kernel values -- the u and v values with the checkerboard sign (-1)^(p+q)
+// folded in, and the w values -- and the chunk's grid rows (wrapped, in the
+// grid's row order, times the row length) and columns.  Then per w-plane k
+// each warp takes the items reaching k whose chunk index is congruent to the
+// warp modulo the warp count (an item always meets the same warp, so its
+// running sums need no barrier between planes), two items at a time: lane
+// (g, a) reads column a of the item's support rows of its pols straight
+// from the grid -- the eight lanes of a group read eight adjacent cells of
+// one row, one 64-byte segment -- weights them by the v values, folds in its
+// u value, and the lanes of a group are summed by shuffles.  The tile's
+// cells of one plane stay in L1 while the chunk's items pass over them.
+// Per item-plane: W reads and 2 W FMAs per lane and one shuffle reduction,
+// with no shared-memory staging and no per-plane barrier.  The epilogue
+// (thread i, item i) rotates back by exp(+2 pi i w tc), conjugates mirrored
+// items, applies the pol-frame matrix and weights and writes (the item's
+// first batch) or accumulates (later batches).
+template <int NP, int AW>
+__device__ __forceinline__ void degrid_warp_chunk(
     const Geom &g, const ItemF *__restrict__ items, const Chunk ch, int b0, int nb,
     const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
-    const float *__restrict__ wgt, const PolMat &pm, const RowPerm &rp, float2 *stage,
-    float *skv, int *s_rowoff, int *s_col) {
-  constexpr int PP = degrid_pass_pols(NP);
-  const int T = g.T;
-  const int SW = T + WT - 1, rowf2 = lane_row(PP, SW), pstride = SW * rowf2;
+    const float *__restrict__ wgt, const PolMat &pm, const RowPerm &rp, float *kc, float2 *sacc,
+    int *s_first, int *s_rowoff, int *s_col) {
+  using LM = LaneMap<NP, AW>;
+  constexpr int KS = kcache_stride(AW);
+  constexpr int kMaxRows = (AW + LM::RS - 1) / LM::RS;
+  const int W = g.W, T = g.T, SW = T + W - 1;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  (void)lane;
-  const float scale_u = 2.f / (float)WT;
+  const LM lm(lane);
+  const bool lane_in = lm.a < W;
+  const float scale_u = 2.f / (float)W;
   const float beta = (float)g.beta;
   const int ntiles = g.ntu * g.ntv;
   const int64_t plane = (int64_t)g.ngx * g.ngy;
-  const int wk = g.do_w ? WT : 1;
-  {
-    const int slab = (int)(ch.bucket / (uint32_t)ntiles);
-    const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
-    const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
-    const int kbase = slab * g.S;
-    // a chunk's items run in order of first w-plane (sort_key): its planes
-    // span from its first item's first plane to its last item's last
-    const int lk_first = (int)((items[ch.begin].loc >> 16) & 0xffu);
-    const int lk_last = (int)((items[ch.end - 1].loc >> 16) & 0xffu);
-    const int k_lo = max(kbase + lk_first, b0);
-    const int k_hi = min(min(kbase + lk_last + WT, g.nplanes), b0 + nb);
-    if (k_lo >= k_hi) return;  // (block-uniform) no item reaches this batch's planes
-    const int n = (int)(ch.end - ch.begin);
-    const bool direct = n * WT * WT < SW * SW;
-    const bool has = (int)threadIdx.x < n;
-    ItemF it = items[ch.begin + (has ? threadIdx.x : 0)];
+  const int wk = g.do_w ? W : 1;
+  const int slab = (int)(ch.bucket / (uint32_t)ntiles);
+  const int tile = (int)(ch.bucket - (uint32_t)slab * ntiles);
+  const int tv = tile / g.ntu, tu = tile - tv * g.ntu;
+  const int kbase = slab * g.S;
+  // a chunk's items run in order of first w-plane (sort_key): its planes
+  // span from its first item's first plane to its last item's last
+  const int lk_first = (int)((items[ch.begin].loc >> 16) & 0xffu);
+  const int lk_last = (int)((items[ch.end - 1].loc >> 16) & 0xffu);
+  const int k_lo = max(kbase + lk_first, b0);
+  const int k_hi = min(min(kbase + lk_last + wk, g.nplanes), b0 + nb);
+  if (k_lo >= k_hi) return;  // (block-uniform) no item reaches this batch's planes
+  const int n = (int)(ch.end - ch.begin);
+  for (int i = threadIdx.x; i < 2 * SW; i += kThreads) {
+    if (i < SW) {
+      int q = tv * T + i;
+      while (q >= g.ngy) q -= g.ngy;
+      s_rowoff[i] = rp.row(q) * g.ngx;
+    } else {
+      int pc = tu * T + (i - SW);
+      while (pc >= g.ngx) pc -= g.ngx;
+      s_col[i - SW] = pc;
+    }
+  }
+  const int tpar = ((tu + tv) * T) & 1;  // checkerboard parity of the tile origin
+  for (int jj = threadIdx.x; jj < n; jj += kThreads) {
+    const ItemF it = items[ch.begin + jj];
+    float *c = kc + jj * KS;
+    c[0] = __uint_as_float(it.loc);
     const int lu = (int)(it.loc & 0xffu), lv = (int)((it.loc >> 8) & 0xffu);
+#pragma unroll
+    for (int a = 0; a < AW; ++a) {
+      const bool in = a < W;
+      const float x = in ? es_kernel(((float)a - it.du) * scale_u, beta) : 0.f;
+      const float y = in ? es_kernel(((float)a - it.dv) * scale_u, beta) : 0.f;
+      c[4 + a] = ((lu + a + tpar) & 1) ? -x : x;
+      c[4 + AW + a] = ((lv + a) & 1) ? -y : y;
+      c[4 + 2 * AW + a] = in ? (g.do_w ? es_kernel(((float)a - it.dwf) * scale_u, beta) : 1.f)
+                             : 0.f;
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) sacc[jj * NP + p] = make_float2(0.f, 0.f);
+    // s_first[l] = the first item with lk >= l (the items reaching plane k
+    // are then one run)
+    const int lk = (int)((it.loc >> 16) & 0xffu);
+    const int lkp = jj == 0 ? -1 : (int)((items[ch.begin + jj - 1].loc >> 16) & 0xffu);
+    for (int q = lkp + 1; q <= lk; ++q) s_first[q] = jj;
+    if (jj == n - 1)
+      for (int q = lk + 1; q <= g.S; ++q) s_first[q] = n;
+  }
+  __syncthreads();
+  for (int k = k_lo; k < k_hi; ++k) {
+    const float2 *gplane = grid + (int64_t)(k - b0) * NP * plane;
+    const int lk_lo = max(0, k - kbase - wk + 1), lk_hi = min(g.S - 1, k - kbase);
+    if (lk_lo > lk_hi) continue;
+    const int jlo = s_first[lk_lo], jhi = s_first[lk_hi + 1];
+    // this warp's items: index congruent to the warp
+    for (int j0 = jlo + ((warp - jlo) % kWarps + kWarps) % kWarps; j0 < jhi;
+         j0 += 2 * kWarps) {
+      const bool two = j0 + kWarps < jhi;  // warp-uniform
+      float sr[2][LM::NPL], si[2][LM::NPL], kf[2];
+      float kv[2][LM::RS == 1 ? AW : 1];
+      const float2 *base[2][LM::NPL];
+      const float *kjs[2];
+      int lvs[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int jj = (u == 1 && two) ? j0 + kWarps : j0;
+        const float *kj = kc + jj * KS;
+        kjs[u] = kj;
+        const uint32_t loc = __float_as_uint(kj[0]);
+        const int lu = (int)(loc & 0xffu);
+        lvs[u] = (int)((loc >> 8) & 0xffu);
+        const int aw = k - (kbase + (int)((loc >> 16) & 0xffu));  // in [0, wk) here
+        kf[u] = kj[4 + 2 * AW + aw] * kj[4 + lm.a];               // kw(aw) ku(a), signed
+        if constexpr (LM::RS == 1) {
+#pragma unroll
+          for (int q = 0; q < AW; q += 4) {
+            const float4 t = *reinterpret_cast<const float4 *>(kj + 4 + AW + q);
+            kv[u][q] = t.x;
+            kv[u][q + 1] = t.y;
+            kv[u][q + 2] = t.z;
+            kv[u][q + 3] = t.w;
+          }
+        }
+        const int col = s_col[lu + (lane_in ? lm.a : 0)];
+#pragma unroll
+        for (int i = 0; i < LM::NPL; ++i) {
+          base[u][i] = gplane + lm.pol(i) * plane + col;
+          sr[u][i] = 0.f;
+          si[u][i] = 0.f;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kMaxRows; ++r) {
+        if (LM::RS == 1 && r >= W) break;  // warp-uniform
+        const int b = lm.r0 + r * LM::RS;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (u == 1 && !two) break;  // warp-uniform
+          if (b < W && lane_in) {
+            float kvb;
+            if constexpr (LM::RS == 1)
+              kvb = kv[u][r];
+            else
+              kvb = kjs[u][4 + AW + b];
+            const int ro = s_rowoff[lvs[u] + b];
+#pragma unroll
+            for (int i = 0; i < LM::NPL; ++i) {
+              const float2 v = __ldg(base[u][i] + ro);
+              sr[u][i] += kvb * v.x;
+              si[u][i] += kvb * v.y;
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (u == 1 && !two) break;  // warp-uniform
+        const int jj = u == 1 ? j0 + kWarps : j0;
+#pragma unroll
+        for (int i = 0; i < LM::NPL; ++i) {
+          float xr = sr[u][i] * kf[u], xi = si[u][i] * kf[u];
+#pragma unroll
+          for (int o = 1; o < AW; o <<= 1) {
+            xr += __shfl_xor_sync(0xffffffffu, xr, o);
+            xi += __shfl_xor_sync(0xffffffffu, xi, o);
+          }
+          if (NP < LM::G) {  // groups sharing a pol hold different rows
+#pragma unroll
+            for (int o = AW * NP; o < 32; o <<= 1) {
+              xr += __shfl_xor_sync(0xffffffffu, xr, o);
+              xi += __shfl_xor_sync(0xffffffffu, xi, o);
+            }
+          }
+          if (lm.a == 0 && lm.r0 == 0) {  // only this warp touches item jj
+            float2 &s = sacc[jj * NP + lm.pol(i)];
+            s.x += xr;
+            s.y += xi;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();  // every item's sums complete
+  for (int jj = threadIdx.x; jj < n; jj += kThreads) {
+    const ItemF it = items[ch.begin + jj];
     const int k0 = kbase + (int)((it.loc >> 16) & 0xffu);
-    const int tpar = ((tu + tv) * T) & 1;  // checkerboard parity of the tile origin
-    float ku[WT];
+    if (!(k0 + wk > b0 && k0 < b0 + nb)) continue;
+    float2 v[NP];
+    // a mirrored item (at -uvw) predicts the conjugate
+    const float conj_sign = (it.loc & kLocFlip) ? -1.f : 1.f;
 #pragma unroll
-    for (int a = 0; a < WT; ++a) {
-      const float x = es_kernel(((float)a - it.du) * scale_u, beta);
-      const float y = es_kernel(((float)a - it.dv) * scale_u, beta);
-      ku[a] = ((lu + a + tpar) & 1) ? -x : x;
-      skv[a * kThreads + threadIdx.x] = ((lv + a) & 1) ? -y : y;
+    for (int p = 0; p < NP; ++p) {  // multiply by conj(ph) = exp(+2 pi i w tc)
+      const float2 a = sacc[jj * NP + p];
+      v[p].x = a.x * it.ph.x + a.y * it.ph.y;
+      v[p].y = (a.y * it.ph.x - a.x * it.ph.y) * conj_sign;
     }
-    float2 acc[NP];
+    const size_t vbase = (size_t)it.idx * npv;
+    const bool first = k0 >= b0;
+    for (int q = 0; q < npv; ++q) {
+      float2 o = v[0];
+      if (pm.identity) {
 #pragma unroll
-    for (int p = 0; p < NP; ++p) acc[p] = make_float2(0.f, 0.f);
-    // the sub-grid's grid rows (physical row x ngx, in the row order of the
-    // grid) and columns, wrapped once per chunk for every staged plane
-    if (!direct) {
-      for (int i = threadIdx.x; i < 2 * SW; i += kThreads) {
-        if (i < SW) {
-          int q = tv * T + i;
-          while (q >= g.ngy) q -= g.ngy;
-          s_rowoff[i] = rp.row(q) * g.ngx;
-        } else {
-          int pc = tu * T + (i - SW);
-          while (pc >= g.ngx) pc -= g.ngx;
-          s_col[i - SW] = pc;
+        for (int p = 1; p < NP; ++p)
+          if (p == (q < NP ? q : NP - 1)) o = v[p];
+      } else {
+        float re = 0.f, im = 0.f;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+          const float mr = pm.fre[q * pm.nin + p], mi = pm.fim[q * pm.nin + p];
+          re += mr * v[p].x - mi * v[p].y;
+          im += mr * v[p].y + mi * v[p].x;
         }
+        o = make_float2(re, im);
       }
-      __syncthreads();
-    }
-    // the pols in passes of PP: each pass stages its pols' sub-grids only,
-    // which halves the staging buffers and the per-thread sums for NP = 4
-    // (unrolled: acc stays in registers)
-#pragma unroll
-    for (int pb = 0; pb < NP; pb += PP) {
-      // raw sub-grid of plane k (pols pb .. pb + PP) -> dst, one cp.async
-      // commit group per thread
-      auto stage_plane = [&](int k, float2 *dst) {
-        const float2 *gp = grid + ((int64_t)(k - b0) * NP + pb) * plane;
-        static_assert(PP <= 2, "one or two pols per staging pass");
-        for (int r = warp; r < PP * SW; r += kWarps) {
-          const int pol = r >= SW ? 1 : 0, y = r - pol * SW;
-          const float2 *src = gp + pol * plane + s_rowoff[y];
-          float2 *d = dst + y * rowf2 + pol;
-          for (int x = lane; x < SW; x += 32) cp_async8(d + x * PP, src + s_col[x], true);
-        }
-        cp_async_commit();
-      };
-      if (!direct && k_lo < k_hi) stage_plane(k_lo, stage);
-      for (int k = k_lo; k < k_hi; ++k) {
-        const float2 *gp = grid + ((int64_t)(k - b0) * NP + pb) * plane;
-        const float2 *sg = stage + ((k - k_lo) & 1) * pstride;
-        if (!direct) {
-          // plane k + 1 goes to the other buffer (consumed in iteration k - 1,
-          // released by that iteration's closing barrier)
-          if (k + 1 < k_hi) {
-            stage_plane(k + 1, stage + ((k + 1 - k_lo) & 1) * pstride);
-            cp_async_wait1();
-          } else {
-            cp_async_wait0();
-          }
-          __syncthreads();  // plane k staged by every thread
-        }
-        const int aw = k - k0;
-        if (has && aw >= 0 && aw < wk) {
-          const float fw = g.do_w ? es_kernel(((float)aw - it.dwf) * scale_u, beta) : 1.f;
-          float2 sum[PP];
-#pragma unroll
-          for (int p = 0; p < PP; ++p) sum[p] = make_float2(0.f, 0.f);
-#pragma unroll 1
-          for (int b = 0; b < WT; ++b) {
-            float2 rs[PP];
-#pragma unroll
-            for (int p = 0; p < PP; ++p) rs[p] = make_float2(0.f, 0.f);
-            if (direct) {
-              int q = tv * T + lv + b;
-              while (q >= g.ngy) q -= g.ngy;
-              const float2 *row = gp + (int64_t)rp.row(q) * g.ngx;
-#pragma unroll
-              for (int a = 0; a < WT; ++a) {
-                int pc = tu * T + lu + a;
-                while (pc >= g.ngx) pc -= g.ngx;
-#pragma unroll
-                for (int p = 0; p < PP; ++p) {
-                  const float2 v = row[p * plane + pc];
-                  rs[p].x += ku[a] * v.x;
-                  rs[p].y += ku[a] * v.y;
-                }
-              }
-            } else {
-              // a cell's PP values are contiguous: 16-byte loads of two pols
-              const float2 *row = sg + (lv + b) * rowf2 + lu * PP;
-#pragma unroll
-              for (int a = 0; a < WT; ++a) {
-                if constexpr (PP == 1) {
-                  const float2 v = row[a];
-                  rs[0].x += ku[a] * v.x;
-                  rs[0].y += ku[a] * v.y;
-                } else {
-#pragma unroll
-                  for (int pp = 0; pp < PP / 2; ++pp) {
-                    const float4 v = *reinterpret_cast<const float4 *>(row + a * PP + 2 * pp);
-                    rs[2 * pp].x += ku[a] * v.x;
-                    rs[2 * pp].y += ku[a] * v.y;
-                    rs[2 * pp + 1].x += ku[a] * v.z;
-                    rs[2 * pp + 1].y += ku[a] * v.w;
-                  }
-                }
-              }
-            }
-            const float kvb = skv[b * kThreads + threadIdx.x];
-#pragma unroll
-            for (int p = 0; p < PP; ++p) {
-              sum[p].x += kvb * rs[p].x;
-              sum[p].y += kvb * rs[p].y;
-            }
-          }
-#pragma unroll
-          for (int p = 0; p < PP; ++p) {
-            acc[pb + p].x += fw * sum[p].x;
-            acc[pb + p].y += fw * sum[p].y;
-          }
-        }
-        if (!direct) __syncthreads();  // buffer consumed before it is refilled
+      if (wgt) {
+        const float w = wgt[vbase + q];
+        o.x *= w;
+        o.y *= w;
       }
-    }
-    if (has && k0 + wk > b0 && k0 < b0 + nb) {
-      float2 v[NP];
-      // a mirrored item (at -uvw) predicts the conjugate
-      const float conj_sign = (it.loc & kLocFlip) ? -1.f : 1.f;
-#pragma unroll
-      for (int p = 0; p < NP; ++p) {  // multiply by conj(ph) = exp(+2 pi i w tc)
-        v[p].x = acc[p].x * it.ph.x + acc[p].y * it.ph.y;
-        v[p].y = (acc[p].y * it.ph.x - acc[p].x * it.ph.y) * conj_sign;
-      }
-      const size_t base = (size_t)it.idx * npv;
-      const bool first = k0 >= b0;
-      for (int q = 0; q < npv; ++q) {
-        float2 o = v[0];
-        if (pm.identity) {
-#pragma unroll
-          for (int p = 1; p < NP; ++p)
-            if (p == (q < NP ? q : NP - 1)) o = v[p];
-        } else {
-          float re = 0.f, im = 0.f;
-#pragma unroll
-          for (int p = 0; p < NP; ++p) {
-            const float mr = pm.fre[q * pm.nin + p], mi = pm.fim[q * pm.nin + p];
-            re += mr * v[p].x - mi * v[p].y;
-            im += mr * v[p].y + mi * v[p].x;
-          }
-          o = make_float2(re, im);
-        }
-        if (wgt) {
-          const float w = wgt[base + q];
-          o.x *= w;
-          o.y *= w;
-        }
-        if (first) {
-          vis[base + q] = o;
-        } else {
-          float2 prev = vis[base + q];
-          prev.x += o.x;
-          prev.y += o.y;
-          vis[base + q] = prev;
-        }
+      if (first) {
+        vis[vbase + q] = o;
+      } else {
+        float2 prev = vis[vbase + q];
+        prev.x += o.x;
+        prev.y += o.y;
+        vis[vbase + q] = prev;
       }
     }
   }
 }
 
-// CTAs per SM the lane degridders are compiled for (registers <= 80).
-constexpr int kDegridLaneBlocks = 3;
+// CTAs per SM the warp degridders are compiled for: few enough that the
+// CTAs' tiles of one plane fit L1 beside their shared memory.
+constexpr int kDegridWarpBlocks = 3;
 
-template <int NP, int WT>
-__global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
-    k_degrid_lane(const Geom g, const ItemF *__restrict__ items, const Chunk *__restrict__ chunks,
+// Dynamic shared memory of the warp degridder: the item cache, then the
+// per-item sums.
+__host__ __device__ constexpr size_t degrid_warp_smem(int AW, int NP) {
+  return (size_t)kChunkItems * (kcache_stride(AW) * sizeof(float) + NP * sizeof(float2));
+}
+
+template <int NP, int AW>
+__global__ void __launch_bounds__(kThreads, kDegridWarpBlocks)
+    k_degrid_warp(const Geom g, const ItemF *__restrict__ items, const Chunk *__restrict__ chunks,
                   const uint32_t *__restrict__ chunk_off, int b0, int nb,
                   const float2 *__restrict__ grid, float2 *__restrict__ vis, int npv,
                   const float *__restrict__ wgt, const PolMat pm, const RowPerm rp,
                   uint32_t *__restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int SW = g.T + WT - 1, pstride = SW * lane_row(degrid_pass_pols(NP), SW);
-  float2 *stage = reinterpret_cast<float2 *>(smem_raw);          // 2 x [SW][rowf2]
-  float *skv = reinterpret_cast<float *>(stage + 2 * pstride);   // [WT][kThreads]: own kv
-  __shared__ int s_rowoff[kMaxSubSide], s_col[kMaxSubSide];
+  float *kc = reinterpret_cast<float *>(smem_raw);                               // item cache
+  float2 *sacc = reinterpret_cast<float2 *>(kc + kChunkItems * kcache_stride(AW));  // sums
+  __shared__ int s_first[kMaxSlab + 1], s_rowoff[kMaxSubSide], s_col[kMaxSubSide];
+  __shared__ uint32_t s_ci;
   const int ntiles = g.ntu * g.ntv;
-  const int lo = b0 - (g.S + WT - 2);
+  const int wk = g.do_w ? g.W : 1;
+  const int lo = b0 - (g.S + wk - 2);
   const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
   const int s_hi = min(g.nslabs - 1, (b0 + nb - 1) / g.S);
   const uint32_t c_begin = chunk_off[(int64_t)s_lo * ntiles];
   const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
-  __shared__ uint32_t s_ci;
   for (;;) {
     if (threadIdx.x == 0) s_ci = c_begin + atomicAdd(counter, 1u);
     __syncthreads();
     const uint32_t ci = s_ci;
-    __syncthreads();  // every thread has read s_ci
+    __syncthreads();  // every thread has read s_ci (and the last chunk's tables)
     if (ci >= c_end) break;
-    degrid_lane_chunk<NP, WT>(g, items, chunks[ci], b0, nb, grid, vis, npv, wgt, pm, rp, stage,
-                              skv, s_rowoff, s_col);
+    degrid_warp_chunk<NP, AW>(g, items, chunks[ci], b0, nb, grid, vis, npv, wgt, pm, rp, kc,
+                              sacc, s_first, s_rowoff, s_col);
   }
 }
 
-// Many plans' degridding in one persistent launch (FP32 form, one support
-// WT): the work queue is the concatenation of every job's chunk range, as
-// in k_grid_jobs; each CTA takes the next index from one atomic counter and
-// degrids that chunk of its job into the job's visibilities.
-template <int NP, int WT>
-__global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
-    k_degrid_lane_jobs(const __grid_constant__ GridJobs jobs, const PolMat pm,
+// Many plans' degridding in one persistent launch (FP32 form, one lane
+// width): the work queue is the concatenation of every job's chunk range,
+// as in k_grid_jobs; each CTA takes the next index from one atomic counter
+// and degrids that chunk of its job into the job's visibilities.
+template <int NP, int AW>
+__global__ void __launch_bounds__(kThreads, kDegridWarpBlocks)
+    k_degrid_warp_jobs(const __grid_constant__ GridJobs jobs, const PolMat pm,
                        uint32_t *__restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *kc = reinterpret_cast<float *>(smem_raw);
+  float2 *sacc = reinterpret_cast<float2 *>(kc + kChunkItems * kcache_stride(AW));
+  __shared__ int s_first[kMaxSlab + 1], s_rowoff[kMaxSubSide], s_col[kMaxSubSide];
   __shared__ uint32_t s_wbeg[kMaxJobs + 1], s_cbeg[kMaxJobs];
   __shared__ uint32_t s_w;
   __shared__ int s_j;
-  int pstride_max = 0;
-  for (int j = 0; j < jobs.n; ++j) {
-    const int SW = jobs.job[j].g.T + WT - 1;
-    pstride_max = max(pstride_max, SW * lane_row(degrid_pass_pols(NP), SW));
-  }
-  float2 *stage = reinterpret_cast<float2 *>(smem_raw);
-  float *skv = reinterpret_cast<float *>(stage + 2 * pstride_max);
-  __shared__ int s_rowoff[kMaxSubSide], s_col[kMaxSubSide];
   if (threadIdx.x == 0) {
     uint32_t w = 0;
     for (int j = 0; j < jobs.n; ++j) {
       const GridJob &jb = jobs.job[j];
       const Geom &g = jb.g;
       const int ntiles = g.ntu * g.ntv;
-      const int lo = jb.b0 - (g.S + WT - 2);
+      const int wk = g.do_w ? g.W : 1;
+      const int lo = jb.b0 - (g.S + wk - 2);
       const int s_lo = lo <= 0 ? 0 : (lo + g.S - 1) / g.S;
       const int s_hi = min(g.nslabs - 1, (jb.b0 + jb.nb - 1) / g.S);
       const uint32_t c0 = jb.chunk_off[(int64_t)s_lo * ntiles];
@@ -635,65 +639,50 @@ __global__ void __launch_bounds__(kThreads, kDegridLaneBlocks)
     if (w >= total) break;
     const GridJob &jb = jobs.job[j];
     const uint32_t ci = s_cbeg[j] + (w - s_wbeg[j]);
-    degrid_lane_chunk<NP, WT>(jb.g, reinterpret_cast<const ItemF *>(jb.items), jb.chunks[ci],
+    degrid_warp_chunk<NP, AW>(jb.g, reinterpret_cast<const ItemF *>(jb.items), jb.chunks[ci],
                               jb.b0, jb.nb, reinterpret_cast<const float2 *>(jb.grid),
-                              reinterpret_cast<float2 *>(jb.vis), jb.npv, jb.wgt, pm, jb.rp,
-                              stage, skv, s_rowoff, s_col);
+                              reinterpret_cast<float2 *>(jb.vis), jb.npv, jb.wgt, pm, jb.rp, kc,
+                              sacc, s_first, s_rowoff, s_col);
   }
 }
 
-size_t degrid_lane_smem_bytes(const gb_plan *p) {
-  const int SW = p->g.T + p->g.W - 1;
-  return (size_t)2 * SW * lane_row(degrid_pass_pols(p->g.NP), SW) * sizeof(float2) +
-         (size_t)p->g.W * kThreads * sizeof(float);
+size_t degrid_warp_smem_bytes(const gb_plan *p) {
+  return degrid_warp_smem(group_lanes(p->g.W), p->g.NP);
 }
 
-// Launch k_degrid_lane<NP, W> for the plan's support (4..16).
-template <int NP>
-static void launch_degrid_lane(const gb_plan *p, unsigned blocks, size_t smem, cudaStream_t s,
-                               const ItemF *items, const Chunk *chunks, const uint32_t *chunk_off,
-                               int b0, int nb, const float2 *grid, float2 *vis, int npv,
-                               const float *wgt, const PolMat &pm, const RowPerm &rp,
-                               uint32_t *counter) {
-#define GB_DL(WV)                                                                            \
-  case WV:                                                                                   \
-    k_degrid_lane<NP, WV><<<blocks, kThreads, smem, s>>>(p->g, items, chunks, chunk_off, b0, \
-                                                         nb, grid, vis, npv, wgt, pm, rp,    \
-                                                         counter);                           \
-    break;
-  switch (p->g.W) {
-    GB_DL(4) GB_DL(5) GB_DL(6) GB_DL(7) GB_DL(8) GB_DL(9) GB_DL(10) GB_DL(11) GB_DL(12)
-    GB_DL(13) GB_DL(14) GB_DL(15) GB_DL(16)
-    default: break;
-  }
-#undef GB_DL
+// Shared-memory carveout (percent of the SM's maximum) that holds `per_sm`
+// CTAs of `smem` bytes and leaves the rest of the unified array to L1.
+static int degrid_carveout(size_t smem, int per_sm) {
+  int dev = 0, max_smem = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  if (max_smem <= 0) return -1;
+  const size_t need = (size_t)per_sm * (smem + 3072);  // + static and reserved shared memory
+  const int pct = (int)((need * 100 + max_smem - 1) / max_smem);
+  return pct > 100 ? 100 : pct;
 }
 
-template <int NP>
-static int setup_degrid_lane(gb_plan *p) {
-  const size_t smem = degrid_lane_smem_bytes(p);
+template <int NP, int AW>
+static int setup_degrid_warp_aw(gb_plan *p) {
+  const size_t smem = degrid_warp_smem_bytes(p);
+  auto k = k_degrid_warp<NP, AW>;
+  GB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int pct = degrid_carveout(smem, kDegridWarpBlocks);
+  if (pct > 0) GB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
   int per_sm = 0;
-#define GB_DL(WV)                                                                             \
-  case WV:                                                                                    \
-    GB_CUDA(cudaFuncSetAttribute(k_degrid_lane<NP, WV>,                                       \
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));    \
-    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_degrid_lane<NP, WV>,     \
-                                                          kThreads, smem));                   \
-    break;
-  switch (p->g.W) {
-    GB_DL(4) GB_DL(5) GB_DL(6) GB_DL(7) GB_DL(8) GB_DL(9) GB_DL(10) GB_DL(11) GB_DL(12)
-    GB_DL(13) GB_DL(14) GB_DL(15) GB_DL(16)
-    default:
-      set_error("support %d outside 4..16", p->g.W);
-      return GB_ERR_INVALID_ARG;
-  }
-#undef GB_DL
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem));
   if (per_sm < 1) {
-    set_error("k_degrid_lane cannot launch with %zu bytes of shared memory", smem);
+    set_error("k_degrid_warp cannot launch with %zu bytes of shared memory", smem);
     return GB_ERR_INVALID_ARG;
   }
   p->degrid_blocks = per_sm * p->num_sms;
   return GB_OK;
+}
+
+template <int NP>
+static int setup_degrid_warp(gb_plan *p) {
+  return group_lanes(p->g.W) == 8 ? setup_degrid_warp_aw<NP, 8>(p)
+                                  : setup_degrid_warp_aw<NP, 16>(p);
 }
 
 // The predict driver in steps (gb_batch.cu interleaves them across plans):
@@ -786,9 +775,15 @@ static int pred_degrid_impl(gb_plan *p, int bi, const void *wgt, const PolMat &p
   if (prof_on()) degrid_counts<R, NP>(p, bi, npv, wgt != nullptr, &bytes, &updates);
   ProfScope ps(kProfDegrid, s, bytes, updates);
   if constexpr (std::is_same<R, float>::value) {
-    launch_degrid_lane<NP>(p, (unsigned)p->degrid_blocks, degrid_lane_smem_bytes(p), s, items,
-                           chunks, chunk_off, b0, nb, grid, vis_c, npv,
-                           reinterpret_cast<const R *>(wgt), pm, rperm, counters + bi);
+    const size_t smem = degrid_warp_smem_bytes(p);
+    if (group_lanes(g.W) == 8)
+      k_degrid_warp<NP, 8><<<p->degrid_blocks, kThreads, smem, s>>>(
+          g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv, reinterpret_cast<const R *>(wgt),
+          pm, rperm, counters + bi);
+    else
+      k_degrid_warp<NP, 16><<<p->degrid_blocks, kThreads, smem, s>>>(
+          g, items, chunks, chunk_off, b0, nb, grid, vis_c, npv, reinterpret_cast<const R *>(wgt),
+          pm, rperm, counters + bi);
   } else {
     const size_t smem = tile_smem_bytes(p);
     if (group_lanes(g.W) == 8)
@@ -881,51 +876,38 @@ int launch_degrid_jobs(const GridJobs &jobs, const PolMat &pm, int num_sms, uint
     set_error("launch_degrid_jobs: %d jobs (1..%d)", jobs.n, kMaxJobs);
     return GB_ERR_INVALID_ARG;
   }
-  const int NP = jobs.job[0].g.NP, W = jobs.job[0].g.W;
-  int pstride = 0;
+  const int NP = jobs.job[0].g.NP, AW = group_lanes(jobs.job[0].g.W);
   for (int j = 0; j < jobs.n; ++j) {
     const Geom &g = jobs.job[j].g;
-    if (g.NP != NP || g.W != W) {
-      set_error("launch_degrid_jobs: jobs of one launch share NP and the support");
+    if (g.NP != NP || group_lanes(g.W) != AW) {
+      set_error("launch_degrid_jobs: jobs of one launch share NP and the lane width");
       return GB_ERR_INVALID_ARG;
     }
-    const int SW = g.T + W - 1;
-    pstride = std::max(pstride, SW * lane_row(degrid_pass_pols(NP), SW));
   }
-  const size_t smem = (size_t)2 * pstride * sizeof(float2) + (size_t)W * kThreads * sizeof(float);
+  const size_t smem = degrid_warp_smem(AW, NP);
   ProfScope ps(kProfDegrid, s, bytes, updates);
-#define GB_DJ(NPV, WV)                                                                        \
-  case WV: {                                                                                  \
-    auto k = k_degrid_lane_jobs<NPV, WV>;                                                     \
+#define GB_DJ(NPV, AWV)                                                                       \
+  {                                                                                           \
+    auto k = k_degrid_warp_jobs<NPV, AWV>;                                                    \
     GB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));  \
+    const int pct = degrid_carveout(smem, kDegridWarpBlocks);                                 \
+    if (pct > 0)                                                                              \
+      GB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, pct));  \
     int per_sm = 0;                                                                           \
     GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem));       \
     if (per_sm < 1) {                                                                         \
-      set_error("k_degrid_lane_jobs cannot launch with %zu bytes of shared memory", smem);   \
+      set_error("k_degrid_warp_jobs cannot launch with %zu bytes of shared memory", smem);   \
       return GB_ERR_INVALID_ARG;                                                              \
     }                                                                                         \
     k<<<per_sm * num_sms, kThreads, smem, s>>>(jobs, pm, counter);                           \
-    break;                                                                                    \
   }
-#define GB_DJ_NP(NPV)                                                                  \
-  switch (W) {                                                                         \
-    GB_DJ(NPV, 4) GB_DJ(NPV, 5) GB_DJ(NPV, 6) GB_DJ(NPV, 7) GB_DJ(NPV, 8) GB_DJ(NPV, 9)  \
-    GB_DJ(NPV, 10) GB_DJ(NPV, 11) GB_DJ(NPV, 12) GB_DJ(NPV, 13) GB_DJ(NPV, 14)          \
-    GB_DJ(NPV, 15) GB_DJ(NPV, 16)                                                        \
-    default:                                                                             \
-      set_error("support %d outside 4..16", W);                                          \
-      return GB_ERR_INVALID_ARG;                                                         \
-  }
-  if (NP == 1) {
-    GB_DJ_NP(1)
-  } else if (NP == 2) {
-    GB_DJ_NP(2)
+  if (AW == 8) {
+    if (NP == 1) GB_DJ(1, 8) else if (NP == 2) GB_DJ(2, 8) else GB_DJ(4, 8)
   } else {
-    GB_DJ_NP(4)
+    if (NP == 1) GB_DJ(1, 16) else if (NP == 2) GB_DJ(2, 16) else GB_DJ(4, 16)
   }
-#undef GB_DJ_NP
 #undef GB_DJ
-  GB_LAUNCH_CHECK("k_degrid_lane_jobs");
+  GB_LAUNCH_CHECK("k_degrid_warp_jobs");
   return GB_OK;
 }
 
@@ -965,7 +947,7 @@ static int setup_degrid_aw(gb_plan *p) {
 
 template <typename R, int NP>
 static int setup_degrid_impl(gb_plan *p) {
-  if constexpr (std::is_same<R, float>::value) return setup_degrid_lane<NP>(p);
+  if constexpr (std::is_same<R, float>::value) return setup_degrid_warp<NP>(p);
   return group_lanes(p->g.W) == 8 ? setup_degrid_aw<R, NP, 8>(p)
                                   : setup_degrid_aw<R, NP, 16>(p);
 }
