@@ -244,15 +244,13 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS, 3)
   float2 *plane = grid + (int64_t)blockIdx.z * cg.plane;
   load_twiddles<N1, 1>(tw, twn, cg.n);
   float2 x[M];
-  // rows outside the occupancy mask were never zeroed (nor gridded): they
-  // read as zero without a grid load (the mask bytes come first, from L1)
-  bool used[M];
-#pragma unroll
-  for (int m = 0; m < M; ++m) used[m] = ok && cg.row_used(blockIdx.z, cg.N2 * (t + T * m) + q2);
 #pragma unroll
   for (int m = 0; m < M; ++m) {
+    // rows outside the occupancy mask were never zeroed (nor gridded): load
+    // unconditionally (mask and data loads overlap) and select zero
     const int row = cg.N2 * (t + T * m) + q2;
-    x[m] = used[m] ? plane[(int64_t)row * cg.ngx + p] : make_float2(0.f, 0.f);
+    const float2 v = ok ? plane[(int64_t)row * cg.ngx + p] : make_float2(0.f, 0.f);
+    x[m] = cg.row_used(blockIdx.z, row) ? v : make_float2(0.f, 0.f);
   }
   __syncthreads();
   float2 y[M / T][T];
@@ -483,16 +481,11 @@ __global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 3)
   float2 y[M / T][T];
   col_dft<N2, -1>(x, xb, tw, t, c, y);
   if (ok) {
-    // physical row N2 k1 + o holds logical row k1 + N1 o; rows outside the
-    // occupancy mask are never read (not degridded, not row-transformed)
 #pragma unroll
     for (int ii = 0; ii < M / T; ++ii)
 #pragma unroll
-      for (int k2 = 0; k2 < T; ++k2) {
-        const int o = t + T * ii + M * k2;
-        if (cg.row_used(blockIdx.z, k1 + cg.N1 * o))
-          plane[(int64_t)(cg.N2 * k1 + o) * cg.ngx + p] = y[ii][k2];
-      }
+      for (int k2 = 0; k2 < T; ++k2)
+        plane[(int64_t)(cg.N2 * k1 + t + T * ii + M * k2) * cg.ngx + p] = y[ii][k2];
   }
 }
 
