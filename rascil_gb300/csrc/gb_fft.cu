@@ -501,7 +501,13 @@ __global__ void __launch_bounds__(ColShape<N2>::THREADS, N2 >= 256 ? 1 : 3)
 //           R3-point DFT, giving X[k1 + R1 k1' + R1 R2 k2'].
 // Input columns outside [in_lo, in_hi) are taken as zero (predict: only the
 // image columns hold data) and only outputs in [out_lo, out_hi) are stored
-// (invert: only the image columns are needed).  Rows whose (plane, row
+// (invert: only the image columns are needed).  The first N/2 input cells of
+// the next row stream into a shared-memory stage by one bulk copy (mbarrier
+// completion) while the current row's passes 2 and 3 and its stores run;
+// the rest of the input (invert's second half) is loaded directly, its next
+// row prefetched into L2.  A staging wait past its limit records
+// kErrTmaTimeout in *status, waits once more (bounded) for the copy in
+// flight and returns.  Rows whose (plane, row
 // tile) is empty in the occupancy mask are skipped: an invert row there is
 // zero (nothing gridded), a predict row there is never degridded.
 template <int N> struct RowShape;
@@ -523,6 +529,7 @@ struct RowArgs {
   int ngy, NP, b0, T, ntv;
   int perm_s1, perm_s2;      // predict rows: logical row of physical r, or -1
   int in_lo, in_hi, out_lo, out_hi;
+  uint32_t *status;          // kErrTmaTimeout when a staging wait runs past its limit
 };
 
 template <int N, int S>
@@ -533,11 +540,26 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
   constexpr int TN = R2 * R3;  // pass-1 units
   constexpr int NA = N / 128;  // two-level twiddle table: w^m = A[m >> 7] B[m & 127]
   static_assert(TN == TH, "one pass-1 unit per thread");
+  constexpr int NH = N / 2;  // staged input cells per row
   extern __shared__ __align__(16) float2 smem[];
   float2 *ex = smem;                        // exchange: max(R1 (TN + 1), N) cells
   float2 *ta = smem + R1 * (TN + 1);        // [NA]
   float2 *tb = ta + NA;                     // [128]
   float2 *t2 = tb + 128;                    // [TN]: w_TN^m = w_N^(R1 m)
+  float2 *stg = t2 + TN;                    // [NH]: the next row's first input cells
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ int s_abort;
+  // staged: input elements m in [m_lo, m_hi) of pass 1 (col = t + TN m), so
+  // whole multiples of TN cells (always so for the image-column ranges)
+  const int st_lo = ra.in_lo;
+  const int st_n = (st_lo % TN == 0 && ra.in_hi % TN == 0) ? min(ra.in_hi - ra.in_lo, NH) : 0;
+  const int m_lo = st_lo / TN, m_hi = (st_lo + st_n) / TN;
+  const unsigned st_bytes = (unsigned)st_n * (unsigned)sizeof(float2);
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar, 1);
+    s_abort = 0;
+    fence_mbarrier_init();
+  }
   for (int i = threadIdx.x; i < NA + 128; i += TH) {
     const float2 w = ra.twx[i < NA ? i * 128 : i - NA];
     (i < NA ? ta[i] : tb[i - NA]) = S > 0 ? w : conjf2(w);
@@ -562,23 +584,42 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
     }
     return row;
   };
+  // the unstaged input of a row, prefetched into L2
   auto prefetch_row = [&](int64_t row) {
-    if (threadIdx.x == 0 && row < ra.nrows)
-      prefetch_l2(ra.grid + row * N + ra.in_lo, (unsigned)((ra.in_hi - ra.in_lo) * sizeof(float2)));
+    if (threadIdx.x == 0 && row < ra.nrows && st_lo + st_n < ra.in_hi)
+      prefetch_l2(ra.grid + row * N + st_lo + st_n,
+                  (unsigned)((ra.in_hi - st_lo - st_n) * sizeof(float2)));
+  };
+  // the staged input of a row (thread 0; the stage's earlier generic reads
+  // are ordered before the copy by the barrier and the proxy fence)
+  auto stage_row = [&](int64_t row) {
+    fence_proxy_async();
+    mbar_expect_tx(&s_bar, st_bytes);
+    bulk_load(stg, ra.grid + row * N + st_lo, st_bytes, &s_bar);
   };
   const int t = threadIdx.x;
   int64_t row = blockIdx.x;
   if (row < ra.nrows && !used(row)) row = next_used(row);
+  __syncthreads();  // the barrier's initialisation before any wait on it
+  if (threadIdx.x == 0 && row < ra.nrows && st_n) stage_row(row);
   prefetch_row(row);
-  for (; row < ra.nrows; row = next_used(row)) {
-    prefetch_row(next_used(row));
+  unsigned phase = 0;
+  for (; row < ra.nrows;) {
+    const int64_t next = next_used(row);
+    prefetch_row(next);
     float2 *rp = ra.grid + row * N;
+    if (st_n) {
+      if (!mbar_wait(&s_bar, phase)) s_abort = 1;
+      phase ^= 1u;
+    }
     // pass 1
     float2 x[R1];
 #pragma unroll
     for (int m = 0; m < R1; ++m) {
       const int col = t + TN * m;
-      x[m] = (col >= ra.in_lo && col < ra.in_hi) ? rp[col] : make_float2(0.f, 0.f);
+      x[m] = (m >= m_lo && m < m_hi)
+                 ? stg[t + TN * (m - m_lo)]
+                 : ((col >= ra.in_lo && col < ra.in_hi) ? rp[col] : make_float2(0.f, 0.f));
     }
     dft<R1, S>(x);
     {
@@ -601,7 +642,15 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
         ex[k1 * (TN + 1) + t] = v;
       }
     }
-    __syncthreads();
+    __syncthreads();  // pass-1 exchange written; the stage read by every thread
+    if (s_abort) {
+      if (threadIdx.x == 0) {
+        atomicOr(ra.status, kErrTmaTimeout);
+        mbar_wait(&s_bar, phase ^ 1u);  // (bounded) the copy still in flight
+      }
+      return;
+    }
+    if (threadIdx.x == 0 && next < ra.nrows && st_n) stage_row(next);
     // pass 2: units u = k1 + R1 s
     constexpr int U2 = R1 * R3 / TH;
     float2 y[U2][R2];
@@ -638,6 +687,7 @@ __global__ void __launch_bounds__(RowShape<N>::THREADS, RowShape<N>::MINB)
       }
     }
     __syncthreads();  // exchange slots free for the next row
+    row = next;
   }
 }
 
@@ -905,7 +955,7 @@ bool row_kernel_fits(int n) { return n == 4096 || n == 8192 || n == 16384; }
 template <int N> constexpr size_t rows_smem() {
   using RS = RowShape<N>;
   return sizeof(float2) *
-         ((size_t)RS::R1 * (RS::R2 * RS::R3 + 1) + N / 128 + 128 + RS::R2 * RS::R3);
+         ((size_t)RS::R1 * (RS::R2 * RS::R3 + 1) + N / 128 + 128 + RS::R2 * RS::R3 + N / 2);
 }
 
 template <int N, int S> static int rows_occupancy(int *per_sm) {
@@ -946,6 +996,7 @@ int run_rows(gb_plan *p, void *grid, int b0, int nb, int dir, cudaStream_t s) {
   ra.b0 = b0;
   ra.T = g.T;
   ra.ntv = g.ntv;
+  ra.status = p->status_word();
   if (dir > 0) {  // invert: full rows in, image columns out
     ra.perm_s1 = -1;
     ra.perm_s2 = 0;
