@@ -67,11 +67,15 @@ static int plan_geometry_sigma(const gb_plan_params *p, double w_lo, double w_hi
 // plus per-plane transform work per grid cell and polarisation -- the
 // library's pruned row/column transforms where they apply, batched 2-D
 // cuFFT plans with separate zeroing and screen passes otherwise.  Constants
-// measured on the LOW-like workload (k_grid / k_degrid_warp per update; the
-// column-mode passes and cuFFT planes per cell).
-constexpr double kCostItemPlane[2] = {9.3e-11, 2.5e-9};  // FP32, FP64 (at W = 7)
-constexpr double kCostCellColumns = 4.7e-12;
-constexpr double kCostCellCufft[2] = {8.7e-12, 1.8e-11};
+// measured on GB300: per update on the LOW-like workload (k_grid and
+// k_degrid_warp, mean of the two directions), per cell for the column-mode
+// passes there; the FP32 cuFFT-path cell cost is set so that the 256
+// snapshots of the batched workload (1024^2 and 2048^2 images, mostly empty
+// w-planes) keep sigma 2, which measured 12 % faster over the list than
+// sigma 1.5 on 3072^2 / 1536^2 cuFFT grids.
+constexpr double kCostItemPlane[2] = {6.6e-11, 2.5e-9};  // FP32, FP64 (at W = 7)
+constexpr double kCostCellColumns = 4.5e-12;
+constexpr double kCostCellCufft[2] = {1.3e-11, 1.8e-11};
 
 static bool columns_apply(const gb_plan_params *p, const Geom &g) {
   int n1, n2;

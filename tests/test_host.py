@@ -297,14 +297,20 @@ def test_planner_geometry_matches_oracle_other_sigmas(sigma):
 def test_planner_chooses_oversampling_by_cost():
     """With sigma 0 the planner weighs gridding work (W^3 per item) against
     per-plane transform work: a wide field with few visibilities and many
-    w-planes takes the smallest oversampling its form allows (1.5 for FP32,
-    whose grid rounding sigma 1.25's edge correction would amplify beyond
-    epsilon), a dense narrow field (the LOW-like workload) keeps sigma 2 and
-    the library's own transforms; an explicit sigma is kept."""
+    w-planes whose image side is not a power of two (cuFFT transforms at
+    every oversampling) takes the smallest oversampling its form allows
+    (1.5 for FP32, whose grid rounding sigma 1.25's edge correction would
+    amplify beyond epsilon); with a power-of-two side the FP32 form keeps
+    sigma 2, whose grids take the library's pruned column transforms
+    (measured faster than sigma 1.5's smaller cuFFT grids); a dense narrow
+    field (the LOW-like workload) keeps sigma 2; an explicit sigma is kept."""
     from rascil_gb300.wgridder import plan_geometry
-    wide = plan_geometry(2048, 2048, 5.8e-4, 5.8e-4, 1e-5, True, -700.0, 700.0, nrows=100000,
+    wide = plan_geometry(1800, 1800, 6.6e-4, 6.6e-4, 1e-5, True, -700.0, 700.0, nrows=100000,
                          nchan=2, precision="fp32")
     assert wide["sigma"] == 1.5 and wide["fft_mode"] == 1  # 1.25 is below the FP32 form's
+    wide2 = plan_geometry(2048, 2048, 5.8e-4, 5.8e-4, 1e-5, True, -700.0, 700.0, nrows=100000,
+                          nchan=2, precision="fp32")
+    assert wide2["sigma"] == 2.0 and wide2["fft_mode"] == 2
     wide64 = plan_geometry(2048, 2048, 5.8e-4, 5.8e-4, 1e-7, True, -700.0, 700.0, nrows=100000,
                            nchan=2, precision="fp64")
     assert wide64["sigma"] == 1.25
