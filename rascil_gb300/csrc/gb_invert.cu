@@ -179,79 +179,130 @@ template <> struct GridSmem<double> {
   static constexpr bool kCache = false;
 };
 
-// The FP32 gridder's spread of the items reaching plane k (chunk-relative
-// [jj_lo, jj_hi), all with their w-support on k) into the fixed-point
-// sub-grid: two items per warp iteration (independent chains of atomics),
-// kernel values from the item cache -- a lane's u value folded into its
-// values once, the v values of every support row by 16-byte broadcast
-// loads -- then per support row and part one multiply, one conversion and
-// one shared atomic.
+// The FP32 gridder's spread in integer arithmetic.  For sub-grid chunks
+// the item cache holds every item's v kernel values in Q31 (round(kv 2^31),
+// saturating at kv = 1), and a lane converts its value times its u and w
+// kernel values to fixed point once per item and plane (C = round(2 c), c
+// the value at the chunk's fixed-point scale).  A support row's update is
+// then round(C K / 2^32) = round(kv c): the high word of one 32 x 32 -> 64
+// bit multiply-add with 2^31 as addend, on the integer multiply pipe, where
+// a float product and a float-to-integer conversion per row would load the
+// conversion unit (a quarter-rate pipe) with two instructions per row.  The
+// result is within 1 of round(kv c) in the sub-grid's units, closer than an
+// FP32 product of the same magnitudes (a 24-bit mantissa at up to 2^30).
+__device__ __forceinline__ int q31_mul_round(int c, int k) {
+  int hi;
+  asm("{\n\t.reg .b64 t;\n\t.reg .b32 lo;\n\t"
+      "mad.wide.s32 t, %1, %2, %3;\n\t"
+      "mov.b64 {lo, %0}, t;\n\t}"
+      : "=r"(hi)
+      : "r"(c), "r"(k), "l"(0x80000000LL));
+  return hi;
+}
+
+__device__ __forceinline__ int kernel_q31(float kv) {
+  return __float2int_rn(kv * 2147483648.0f);  // saturates at 2^31 - 1 for kv = 1
+}
+
+// NU (1 or 2) items -- chunk-relative jj0 and jj0 + kWarps -- all with their
+// w-support on plane k, spread by one warp into the fixed-point sub-grid.
+// WC > 0: the support width as a compile-time constant (no per-row
+// predicate beyond the lane's own); WC = 0: W at run time.
+template <int NP, int AW, int WC, int NU>
+__device__ __forceinline__ void spread_q31_step(const LaneMap<NP, AW> &lm, int W, int k,
+                                                int kbase, int jj0,
+                                                const float *__restrict__ kc,
+                                                const float2 *__restrict__ cc, int *acc,
+                                                const TileLayout &L) {
+  using LM = LaneMap<NP, AW>;
+  constexpr int KS = kcache_stride(AW);
+  constexpr int WM = WC > 0 ? WC : AW;                  // rows bound, compile time
+  constexpr int NR = (WM + LM::RS - 1) / LM::RS;        // support rows per lane (at most)
+  constexpr int NK = LM::RS == 1 ? (WM + 3) / 4 * 4 : 1;  // Q31 row values held
+  const bool lane_in = lm.a < W;
+  const int im_off = NP * L.plane;
+  int kq[NU][NK];
+  int cre[NU][LM::NPL], cim[NU][LM::NPL];
+  int *pa[NU];
+  const int *kjs[NU];
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    const int jj = jj0 + u * kWarps;
+    const float *kj = kc + jj * KS;
+    kjs[u] = reinterpret_cast<const int *>(kj);
+    const uint32_t loc = __float_as_uint(kj[0]);
+    const int aw = k - (kbase + (int)((loc >> 16) & 0xffu));  // in [0, W) here
+    const float f = 2.f * kj[4 + 2 * AW + aw] * kj[4 + lm.a];   // 2 kw(aw) ku(a)
+    if constexpr (LM::RS == 1) {
+#pragma unroll
+      for (int q = 0; q < NK; q += 4) {
+        const int4 t = *reinterpret_cast<const int4 *>(kj + 4 + AW + q);
+        kq[u][q] = t.x;
+        kq[u][q + 1] = t.y;
+        kq[u][q + 2] = t.z;
+        kq[u][q + 3] = t.w;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < LM::NPL; ++i) {
+      const float2 v = cc[jj * NP + lm.pol(i)];
+      cre[u][i] = __float2int_rn(v.x * f);
+      cim[u][i] = __float2int_rn(v.y * f);
+    }
+    const int lu = (int)(loc & 0xffu), lv = (int)((loc >> 8) & 0xffu);
+    pa[u] = acc + (lv + lm.r0) * L.pitch + lu + lm.a;
+  }
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    const int b = lm.r0 + r * LM::RS;
+    const bool on = (WC > 0 && LM::RS == 1) ? lane_in : (b < W && lane_in);
+    if (on) {
+#pragma unroll
+      for (int u = 0; u < NU; ++u) {
+        const int kb = LM::RS == 1 ? kq[u][r] : kjs[u][4 + AW + b];
+        int *row = pa[u] + r * LM::RS * L.pitch;
+#pragma unroll
+        for (int i = 0; i < LM::NPL; ++i) {
+          int *cell = row + lm.pol(i) * L.plane;
+          atomicAdd(cell, q31_mul_round(cre[u][i], kb));
+          atomicAdd(cell + im_off, q31_mul_round(cim[u][i], kb));
+        }
+      }
+    }
+  }
+}
+
+// The items reaching plane k (chunk-relative [jj_lo, jj_hi), all with their
+// w-support on k): warp w takes items jj_lo + w + 2 kWarps i and the items
+// kWarps after them, two per step (independent chains of atomics), and a
+// last odd item alone.
+template <int NP, int AW, int WC>
+__device__ __forceinline__ void spread_q31(const LaneMap<NP, AW> &lm, int warp, int W, int k,
+                                           int kbase, int jj_lo, int jj_hi,
+                                           const float *__restrict__ kc,
+                                           const float2 *__restrict__ cc, int *acc,
+                                           const TileLayout &L) {
+  int j0 = jj_lo + warp;
+  for (; j0 + kWarps < jj_hi; j0 += 2 * kWarps)
+    spread_q31_step<NP, AW, WC, 2>(lm, W, k, kbase, j0, kc, cc, acc, L);
+  if (j0 < jj_hi) spread_q31_step<NP, AW, WC, 1>(lm, W, k, kbase, j0, kc, cc, acc, L);
+}
+
+// Support widths with a compile-time instance of the spread (the FP32
+// form's defaults: W = 7 at sigma 2 and W = 9 at sigma 1.5 for epsilon
+// 1e-5); other widths take the run-time instance.
 template <int NP, int AW>
 __device__ __forceinline__ void spread_fixed(const LaneMap<NP, AW> &lm, int warp, int W, int k,
                                              int kbase, int jj_lo, int jj_hi,
                                              const float *__restrict__ kc,
                                              const float2 *__restrict__ cc, int *acc,
                                              const TileLayout &L) {
-  using LM = LaneMap<NP, AW>;
-  constexpr int KS = kcache_stride(AW);
-  constexpr int kMaxRows = (AW + LM::RS - 1) / LM::RS;
-  const bool lane_in = lm.a < W;
-  for (int j0 = jj_lo + warp; j0 < jj_hi; j0 += 2 * kWarps) {
-    const bool two = j0 + kWarps < jj_hi;  // warp-uniform
-    float kv[2][LM::RS == 1 ? AW : 1];
-    float2 c[2][LM::NPL];
-    int cell0[2];
-    const float *kjs[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int jj = (u == 1 && two) ? j0 + kWarps : j0;
-      const float *kj = kc + jj * KS;
-      kjs[u] = kj;
-      const uint32_t loc = __float_as_uint(kj[0]);
-      const int aw = k - (kbase + (int)((loc >> 16) & 0xffu));  // in [0, W) here
-      const float f = kj[4 + 2 * AW + aw] * kj[4 + lm.a];        // kw(aw) ku(a)
-      if constexpr (LM::RS == 1) {
-#pragma unroll
-        for (int q = 0; q < AW; q += 4) {
-          const float4 t = *reinterpret_cast<const float4 *>(kj + 4 + AW + q);
-          kv[u][q] = t.x;
-          kv[u][q + 1] = t.y;
-          kv[u][q + 2] = t.z;
-          kv[u][q + 3] = t.w;
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < LM::NPL; ++i) {
-        const float2 v = cc[jj * NP + lm.pol(i)];
-        c[u][i] = make_float2(v.x * f, v.y * f);
-      }
-      const int lu = (int)(loc & 0xffu), lv = (int)((loc >> 8) & 0xffu);
-      cell0[u] = (lv + lm.r0) * L.pitch + lu + lm.a;
-    }
-#pragma unroll
-    for (int r = 0; r < kMaxRows; ++r) {
-      if (LM::RS == 1 && r >= W) break;  // warp-uniform
-      const int b = lm.r0 + r * LM::RS;
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (u == 1 && !two) break;  // warp-uniform
-        if (b < W && lane_in) {
-          float kvb;
-          if constexpr (LM::RS == 1)
-            kvb = kv[u][r];
-          else
-            kvb = kjs[u][4 + AW + b];
-          const int cell = cell0[u] + r * LM::RS * L.pitch;
-#pragma unroll
-          for (int i = 0; i < LM::NPL; ++i) {
-            const int pl = lm.pol(i);
-            fixed_add(&acc[pl * L.plane + cell], to_fixed(kvb * c[u][i].x));
-            fixed_add(&acc[(NP + pl) * L.plane + cell], to_fixed(kvb * c[u][i].y));
-          }
-        }
-      }
-    }
-  }
+  if (AW == 8 && W == 7)
+    spread_q31<NP, AW, AW == 8 ? 7 : 0>(lm, warp, W, k, kbase, jj_lo, jj_hi, kc, cc, acc, L);
+  else if (AW == 16 && W == 9)
+    spread_q31<NP, AW, AW == 16 ? 9 : 0>(lm, warp, W, k, kbase, jj_lo, jj_hi, kc, cc, acc, L);
+  else
+    spread_q31<NP, AW, 0>(lm, warp, W, k, kbase, jj_lo, jj_hi, kc, cc, acc, L);
 }
 
 // Grid one work chunk (up to kChunkItems items of one (w-slab, uv tile)
@@ -345,7 +396,9 @@ __device__ __forceinline__ void grid_chunk(
         for (int a = 0; a < AW; ++a) {
           const bool in = a < W;
           c[4 + a] = in ? es_kernel(((R)a - it.du) * scale_u, beta) : (R)0;
-          c[4 + AW + a] = in ? es_kernel(((R)a - it.dv) * scale_u, beta) : (R)0;
+          // v values: float for direct chunks, Q31 for the sub-grid spread
+          const R kv = in ? es_kernel(((R)a - it.dv) * scale_u, beta) : (R)0;
+          c[4 + AW + a] = direct ? kv : __int_as_float(kernel_q31(kv));
           c[4 + 2 * AW + a] = in ? (g.do_w ? es_kernel(((R)a - it.dwf) * scale_u, beta) : (R)1)
                                  : (R)0;
         }
