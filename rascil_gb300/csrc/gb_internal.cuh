@@ -324,11 +324,11 @@ struct PlaneTurns {
 // words; pitch and the plane stride are chosen so that the lanes of one
 // instruction fall in 32 distinct shared-memory banks.
 
-inline __host__ __device__ int congruent_up(int x, int m) {
+inline __host__ __device__ constexpr int congruent_up(int x, int m) {
   return x + ((((m % 32) - (x % 32)) % 32) + 32) % 32;
 }
 
-inline __host__ __device__ int group_lanes(int W) { return W <= 8 ? 8 : 16; }
+inline __host__ __device__ constexpr int group_lanes(int W) { return W <= 8 ? 8 : 16; }
 
 // Floats per item in the FP32 gridder's shared-memory item cache: the
 // packed location word (padded to 16 bytes), then the u, v and w kernel
@@ -339,14 +339,11 @@ struct TileLayout {
   int SW, pitch, plane;
 };
 
-inline __host__ __device__ TileLayout tile_layout(int T, int W, int NP) {
+inline __host__ __device__ constexpr TileLayout tile_layout(int T, int W, int NP) {
   const int AW = group_lanes(W), G = 32 / AW;
   const int RS = NP >= G ? 1 : G / NP;
-  TileLayout L;
-  L.SW = T + W - 1;
-  L.pitch = congruent_up(L.SW, AW);
-  L.plane = congruent_up(L.SW * L.pitch, AW * RS);
-  return L;
+  const int SW = T + W - 1, pitch = congruent_up(SW, AW);
+  return TileLayout{SW, pitch, congruent_up(SW * pitch, AW * RS)};
 }
 
 template <int NP, int AW>

@@ -155,10 +155,12 @@ __device__ __forceinline__ void batch_slabs(const Geom &g, int b0, int nb, int &
 template <typename R> struct FixedAcc;
 template <> struct FixedAcc<float> {
   using T = int;
+  using T2 = int2;
   static constexpr double kOne = 1073741824.0;  // 2^30
 };
 template <> struct FixedAcc<double> {
   using T = long long;
+  using T2 = longlong2;
   static constexpr double kOne = 2305843009213693952.0;  // 2^61
 };
 __device__ __forceinline__ int to_fixed(float v) { return __float2int_rn(v); }
@@ -290,19 +292,25 @@ __device__ __forceinline__ void spread_q31(const LaneMap<NP, AW> &lm, int warp, 
 
 // Support widths with a compile-time instance of the spread (the FP32
 // form's defaults: W = 7 at sigma 2 and W = 9 at sigma 1.5 for epsilon
-// 1e-5); other widths take the run-time instance.
+// 1e-5); other widths take the run-time instance.  With the default
+// 32-cell tile as well, the sub-grid layout is a compile-time constant, so
+// a support row's atomics address the sub-grid by immediate offsets.
 template <int NP, int AW>
-__device__ __forceinline__ void spread_fixed(const LaneMap<NP, AW> &lm, int warp, int W, int k,
-                                             int kbase, int jj_lo, int jj_hi,
+__device__ __forceinline__ void spread_fixed(const LaneMap<NP, AW> &lm, int warp, int W, int T,
+                                             int k, int kbase, int jj_lo, int jj_hi,
                                              const float *__restrict__ kc,
                                              const float2 *__restrict__ cc, int *acc,
                                              const TileLayout &L) {
-  if (AW == 8 && W == 7)
+  if (AW == 8 && W == 7 && T == 32) {
+    constexpr TileLayout L32 = tile_layout(32, 7, NP);
+    spread_q31<NP, AW, AW == 8 ? 7 : 0>(lm, warp, W, k, kbase, jj_lo, jj_hi, kc, cc, acc, L32);
+  } else if (AW == 8 && W == 7) {
     spread_q31<NP, AW, AW == 8 ? 7 : 0>(lm, warp, W, k, kbase, jj_lo, jj_hi, kc, cc, acc, L);
-  else if (AW == 16 && W == 9)
+  } else if (AW == 16 && W == 9) {
     spread_q31<NP, AW, AW == 16 ? 9 : 0>(lm, warp, W, k, kbase, jj_lo, jj_hi, kc, cc, acc, L);
-  else
+  } else {
     spread_q31<NP, AW, 0>(lm, warp, W, k, kbase, jj_lo, jj_hi, kc, cc, acc, L);
+  }
 }
 
 // Grid one work chunk (up to kChunkItems items of one (w-slab, uv tile)
@@ -419,7 +427,7 @@ __device__ __forceinline__ void grid_chunk(
       const uint32_t j_hi = lk_lo <= lk_hi ? ch.begin + (uint32_t)s_first[lk_hi + 1] : j_lo;
       if constexpr (kCache) {
         if (!direct)
-          spread_fixed<NP, AW>(lm, warp, W, k, kbase, (int)(j_lo - ch.begin),
+          spread_fixed<NP, AW>(lm, warp, W, T, k, kbase, (int)(j_lo - ch.begin),
                                (int)(j_hi - ch.begin), kc, cc, acc, L);
       }
       for (uint32_t j = j_lo + warp; j < j_hi && (!kCache || direct); j += kWarps) {
@@ -518,15 +526,18 @@ __device__ __forceinline__ void grid_chunk(
           const R sgn = ((p + q) & 1) ? -inv : inv;  // the pair's second cell: -sgn
 #pragma unroll
           for (int pol = 0; pol < NP; ++pol) {
-            A *are = acc + pol * L.plane + cell, *aim = acc + (NP + pol) * L.plane + cell;
-            const A re0 = are[0], re1 = are[1], im0 = aim[0], im1 = aim[1];
-            if ((re0 | re1 | im0 | im1) != 0) {
-              are[0] = 0;
-              are[1] = 0;
-              aim[0] = 0;
-              aim[1] = 0;
-              grid_add2(&gplane[pol * plane + (size_t)q * g.ngx + p], sgn * (R)re0,
-                        sgn * (R)im0, -sgn * (R)re1, -sgn * (R)im1);
+            // the pair as one 8-byte (FP32 form) or 16-byte (FP64 form)
+            // shared access: cell is even, and so are the pitch and the
+            // plane stride
+            using A2 = typename FixedAcc<R>::T2;
+            A2 *are = reinterpret_cast<A2 *>(acc + pol * L.plane + cell);
+            A2 *aim = reinterpret_cast<A2 *>(acc + (NP + pol) * L.plane + cell);
+            const A2 re = *are, im = *aim;
+            if ((re.x | re.y | im.x | im.y) != 0) {
+              *are = A2{0, 0};
+              *aim = A2{0, 0};
+              grid_add2(&gplane[pol * plane + (size_t)q * g.ngx + p], sgn * (R)re.x,
+                        sgn * (R)im.x, -sgn * (R)re.y, -sgn * (R)im.y);
             }
           }
         }
