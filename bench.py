@@ -380,7 +380,9 @@ def _ncu_traffic(kernel):
 
 # update-rate rooflines: shared-memory instructions per (item, pol, cell) update
 UPDATE_COST = {"k_grid": ("atomics", 2.0, "2 conflict-free 32-bit shared atomic adds (re, im)"),
-               "k_degrid": ("loads", 1.0, "1 conflict-free 8-byte shared load (complex64)")}
+               "k_degrid": ("loads", 1.0, "1 8-byte grid read (complex64) through the L1 data "
+                                         "pipe, against that pipe's conflict-free 8-byte "
+                                         "shared-load rate")}
 
 
 def roofline(stats, peaks, smem=None):
@@ -1540,12 +1542,14 @@ def workload_config(wl):
 
 # What bounds each kernel of the step (ncu summaries under profiles/).
 KERNEL_BOUND = {
-    "k_grid": "instruction issue around the shared atomics (update rate in roofline.secondary)",
-    "k_degrid": "shared-memory loads and latency (update rate in roofline.secondary)",
+    "k_grid": "shared-memory pipe (atomics and the sub-grid flush) and instruction issue "
+              "(update rate in roofline.secondary)",
+    "k_degrid": "L1 data pipe: grid rows read through L1, plus the item cache in shared memory "
+                "(update rate in roofline.secondary)",
     "k_rows_forward": "instruction issue (DRAM traffic = algorithmic bytes)",
     "k_rows_inverse": "instruction issue (DRAM traffic = algorithmic bytes)",
     "k_col_a_inv": "hbm", "k_col_b_inv": "hbm", "k_col_b_pred": "hbm",
-    "k_col_a_pred": "hbm + FP32 sincos", "grid_zero": "hbm (write only)",
+    "k_col_a_pred": "hbm", "grid_zero": "hbm (write only)",
 }
 
 

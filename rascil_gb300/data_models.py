@@ -284,11 +284,12 @@ class BlockVisibility:
         return _BVisAccessor(self)
 
 
-def copy_visibility(bvis, zero=False, vis=None):
+def copy_visibility(bvis, zero=False, vis=None, skip_vis=False):
     """Deep copy, optionally zeroing vis (``visibility/base.py:105-118``).
     The arrays are copied in parallel; ``vis`` (same shape) becomes the
     copy's visibilities instead of a copy or zeros (predict writes the whole
-    array, so copying or zeroing it first would be wasted)."""
+    array, so copying or zeroing it first would be wasted).  ``skip_vis``
+    leaves the copy's vis unset (``None``) for the caller to fill."""
     if not isinstance(bvis, BlockVisibility):
         new = copy.deepcopy(bvis)
         if vis is not None:
@@ -301,7 +302,9 @@ def copy_visibility(bvis, zero=False, vis=None):
     new._vars = {}
     copied = {}  # arrays shared inside the input stay shared in the copy (as deepcopy)
     for key, arr in bvis._vars.items():
-        if key == "vis" and vis is not None:
+        if key == "vis" and skip_vis:
+            new._vars[key] = DataArray(None)
+        elif key == "vis" and vis is not None:
             assert vis.shape == arr.data.shape
             new._vars[key] = DataArray(vis)
         elif key == "vis" and zero:

@@ -31,6 +31,7 @@ the reference's complex128 path; "fp32" is the fast form), ``device``,
 import logging
 import os
 import threading
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy
 import torch
@@ -211,6 +212,19 @@ def clear_plan_cache(release_memory=False):
             _spare_ws.clear()
 
 
+# Host threads for predict_ng's deep copy of its input (see predict_ng).
+_copy_pool = []
+_copy_pool_lock = threading.Lock()
+
+
+def _host_pool():
+    with _copy_pool_lock:
+        if not _copy_pool:
+            _copy_pool.append(ThreadPoolExecutor(max_workers=4,
+                                                 thread_name_prefix="rascil_gb300_copy"))
+        return _copy_pool[0]
+
+
 def predict_ng(bvis, model, **kwargs):
     """Predict visibilities from a model image (``ng.py:33-133``)."""
     assert image_is_canonical(model)
@@ -240,6 +254,10 @@ def predict_ng(bvis, model, **kwargs):
         if rotates:
             newbvis.attrs["phasecentre"] = model.image_acc.phasecentre
         return newbvis
+    # ng.py:56 deep-copies the input (flags, weights, uvw: several times the
+    # visibilities' bytes); the copy runs on a host thread while the GPU
+    # predicts, and then takes the predicted visibilities as its vis
+    copy_job = _host_pool().submit(copy_visibility, bvis, skip_vis=True)
     uvw = _device_uvw(bvis.uvw.data, device, nan_to_num=True)
     pixels = model["pixels"].data
     out = torch.empty((nrows * nbaselines, vnchan, vnpol), dtype=cdt, device=device)
@@ -269,9 +287,10 @@ def predict_ng(bvis, model, **kwargs):
     result = _to_host(out, out.dtype)
     if result.dtype != vdt:
         result = result.astype(vdt)
-    # ng.py:56 deep-copies the input and zeroes vis; the copy gets the
-    # predicted visibilities directly instead
-    newbvis = copy_visibility(bvis, vis=result)
+    # the zeroed vis of ng.py:56's copy would be overwritten: the copy gets
+    # the predicted visibilities directly instead
+    newbvis = copy_job.result()
+    newbvis["vis"].data = result
     if rotates:
         newbvis.attrs["phasecentre"] = model.image_acc.phasecentre
     return newbvis

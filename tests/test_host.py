@@ -259,6 +259,12 @@ def test_copy_visibility_keeps_aliases_and_takes_given_vis():
     z = copy_visibility(b, zero=True)
     assert numpy.all(z["vis"].data == 0) and numpy.all(b["vis"].data == 1)
     assert c.phasecentre is not None and c.attrs is not b.attrs
+    # predict_ng's form: every array but vis copied, vis left for the caller
+    s = copy_visibility(b, skip_vis=True)
+    assert s["vis"].data is None and s["weight"].data is s["imaging_weight"].data
+    assert s["weight"].data is not w and numpy.all(s["flags"].data == b["flags"].data)
+    s["vis"].data = given
+    assert s.vis.shape == b.vis.shape
 
 
 def test_empty_visibilities_need_no_device():
