@@ -186,11 +186,13 @@ __host__ __device__ inline bool row_flipped(const Geom &g, const double *uvw, ui
 // [-1/2, 1/2]: the w-centring term w tc and, when `shift`, minus the fused
 // phase shift (u, v, w) . s (wavelengths).  Formed in FP64 before the
 // reduction; the FP32 form rounds only the reduced value.
+// `fscale` is f/c per channel (freq / kSpeedOfLight, one IEEE division per
+// channel: the same value a division per item would give).
 __host__ __device__ inline double item_turns(const Geom &g, const double *uvw,
-                                             const double *freq, uint32_t i, bool shift) {
+                                             const double *fscale, uint32_t i, bool shift) {
   const uint32_t r = i / (uint32_t)g.C;
   const uint32_t c = i - r * (uint32_t)g.C;
-  const double k = gb_div(freq[c], kSpeedOfLight);
+  const double k = fscale[c];
   const double sg = row_flipped(g, uvw, r) ? -1.0 : 1.0;  // exact: a sign change
   const double w = sg * gb_mul(uvw[3 * (size_t)r + 2], k);
   double t = g.do_w ? gb_mul(w, g.tc) : 0.0;
@@ -205,11 +207,11 @@ __host__ __device__ inline double item_turns(const Geom &g, const double *uvw,
 }
 
 __host__ __device__ inline void item_coord(const Geom &g, const double *uvw,
-                                           const double *freq, uint32_t i,
+                                           const double *fscale, uint32_t i,
                                            Coord &o) {
   const uint32_t r = i / (uint32_t)g.C;
   const uint32_t c = i - r * (uint32_t)g.C;
-  const double s = gb_div(freq[c], kSpeedOfLight);
+  const double s = fscale[c];
   o.flip = row_flipped(g, uvw, r) ? 1 : 0;
   const double sg = o.flip ? -1.0 : 1.0;  // exact: a sign change
   const double u = sg * gb_mul(uvw[3 * (size_t)r + 0], s);

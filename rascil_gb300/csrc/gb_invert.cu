@@ -325,7 +325,7 @@ __device__ __forceinline__ void grid_chunk(
     const Geom &g, const typename Traits<R>::Item *__restrict__ items,
     const typename Traits<R>::C *__restrict__ cvis, const Chunk ch, int b0, int nb,
     typename Traits<R>::C *__restrict__ grid, typename FixedAcc<R>::T *acc, R *kc,
-    typename Traits<R>::C *cc, double *s_red, R *s_scale, int *s_first) {
+    typename Traits<R>::C *cc, R *s_red, R *s_scale, int *s_first) {
   using C = typename Traits<R>::C;
   using A = typename FixedAcc<R>::T;
   using LM = LaneMap<NP, AW>;
@@ -354,10 +354,13 @@ __device__ __forceinline__ void grid_chunk(
     if (k_lo >= k_hi) return;  // (block-uniform) no item reaches this batch's planes
     const int n = (int)(ch.end - ch.begin);
     const bool direct = n * W * W < SW2;
-    // chunk scale for the fixed-point sub-grid: 2^k / sum_j max |component|
+    // chunk scale for the fixed-point sub-grid: 2^k / sum_j max |component|,
+    // summed in the form's precision (the FP32 form: a sum low by a few
+    // parts in 10^7 at most, against the factor-2 headroom of the 2^30
+    // bound in int32, so no cell sum can overflow)
     R scale = (R)0, inv = (R)0;
     if (!direct) {
-      double m = 0.0;
+      R m = (R)0;
       for (uint32_t j = ch.begin + threadIdx.x; j < ch.end; j += kThreads) {
         R mj = (R)0;
 #pragma unroll
@@ -365,18 +368,18 @@ __device__ __forceinline__ void grid_chunk(
           const C v = cvis[(size_t)j * NP + p];
           mj = fmax(mj, fmax(fabs(v.x), fabs(v.y)));
         }
-        m += (double)mj;
+        m += mj;
       }
       for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
       if (lane == 0) s_red[warp] = m;
       __syncthreads();
-      // one thread forms the scale (FP64 divisions cost 16 cycles a warp
-      // instruction of the FP64 pipe on this part)
+      // one thread forms the scale and its inverse
       if (threadIdx.x == 0) {
-        double S = 0.0;
+        R S = (R)0;
         for (int w = 0; w < kWarps; ++w) S += s_red[w];
-        s_scale[0] = S > 0.0 ? (R)(FixedAcc<R>::kOne / S) : (R)0;
-        s_scale[1] = S > 0.0 ? (R)(S / FixedAcc<R>::kOne) : (R)0;
+        constexpr R kOne = (R)FixedAcc<R>::kOne, kInvOne = (R)(1.0 / FixedAcc<R>::kOne);
+        s_scale[0] = S > (R)0 ? kOne / S : (R)0;
+        s_scale[1] = S > (R)0 ? S * kInvOne : (R)0;
       }
       __syncthreads();
       scale = s_scale[0];
@@ -567,7 +570,7 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t c_end = chunk_off[(int64_t)(s_hi + 1) * ntiles];
   for (int i = threadIdx.x; i < 2 * NP * L.plane; i += kThreads) acc[i] = 0;
   __shared__ uint32_t s_ci;
-  __shared__ double s_red[kWarps];
+  __shared__ R s_red[kWarps];
   __shared__ R s_scale[2];
   __shared__ int s_first[kMaxSlab + 1];
   for (;;) {
@@ -893,7 +896,7 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t s_wbeg[kMaxJobs + 1], s_cbeg[kMaxJobs];
   __shared__ uint32_t s_w;
   __shared__ int s_j;
-  __shared__ double s_red[kWarps];
+  __shared__ float s_red[kWarps];
   __shared__ float s_scale[2];
   __shared__ int s_first[kMaxSlab + 1];
   if (threadIdx.x == 0) {

@@ -431,8 +431,17 @@ __host__ __device__ inline uint32_t sort_key(const Geom &g, const Coord &o) {
   return bucket_of(g, o) * (uint32_t)g.S + (uint32_t)(o.k0 % g.S);
 }
 
+// f/c per channel, once per plan: the per-item coordinates multiply by it
+// (one IEEE division per channel, as the oracle forms freq / c, instead of
+// one per (row, channel) item).
+__global__ void k_freq_scale(const double *__restrict__ freq, int nchan,
+                             double *__restrict__ fscale) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < nchan) fscale[c] = __ddiv_rn(freq[c], kSpeedOfLight);
+}
+
 __global__ void k_count(const Geom g, const double *__restrict__ uvw,
-                        const double *__restrict__ freq, uint32_t *__restrict__ counts,
+                        const double *__restrict__ fscale, uint32_t *__restrict__ counts,
                         uint32_t *__restrict__ keys, uint32_t *__restrict__ ranks) {
   const int lane = threadIdx.x & 31;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -442,7 +451,7 @@ __global__ void k_count(const Geom g, const double *__restrict__ uvw,
     uint32_t key = 0xffffffffu;
     if (active) {
       Coord o;
-      item_coord(g, uvw, freq, (uint32_t)i, o);
+      item_coord(g, uvw, fscale, (uint32_t)i, o);
       key = sort_key(g, o);
     }
     // warp-aggregated increment: one atomic per distinct key in the warp
@@ -461,7 +470,7 @@ __global__ void k_count(const Geom g, const double *__restrict__ uvw,
 
 template <typename R>
 __global__ void k_scatter(const Geom g, const double *__restrict__ uvw,
-                          const double *__restrict__ freq, const uint32_t *__restrict__ keys,
+                          const double *__restrict__ fscale, const uint32_t *__restrict__ keys,
                           const uint32_t *__restrict__ ranks,
                           const uint32_t *__restrict__ offsets,
                           typename Traits<R>::Item *__restrict__ items) {
@@ -469,7 +478,7 @@ __global__ void k_scatter(const Geom g, const double *__restrict__ uvw,
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.nitems; i += stride) {
     Coord o;
-    item_coord(g, uvw, freq, (uint32_t)i, o);
+    item_coord(g, uvw, fscale, (uint32_t)i, o);
     const uint32_t pos = offsets[keys[i]] + ranks[i];
     Item it;
     it.idx = (uint32_t)i;
@@ -481,7 +490,7 @@ __global__ void k_scatter(const Geom g, const double *__restrict__ uvw,
     it.dwf = (R)o.dwf;
     if (g.do_w || g.shifted) {
       // exp(-2 pi i (w tc - (u, v, w) . shift)), reduced in FP64 before the sincos
-      const double turns = item_turns(g, uvw, freq, (uint32_t)i, g.shifted);
+      const double turns = item_turns(g, uvw, fscale, (uint32_t)i, g.shifted);
       R s, c;
       sincos_2pi((R)turns, &s, &c);
       it.ph.x = c;
@@ -850,7 +859,7 @@ static int layout_workspace(gb_plan *p) {
   off = align_up(off + (p->col_fft ? (size_t)g.nplanes * g.ntv : 0));
   p->off_tables = off;
   off = align_up(off + 8 * ((size_t)g.nx + g.ny + 2 * kMaxQuad));
-  // shifted plans keep uvw and freq: a PSF call rebuilds the unshifted factor
+  // shifted plans keep uvw and f/c: a PSF call rebuilds the unshifted factor
   p->off_coords = off;
   off = align_up(off + (g.shifted ? 8 * (3 * (size_t)g.R + g.C) : 0));
   p->off_counters = off;
@@ -873,6 +882,8 @@ static int layout_workspace(gb_plan *p) {
   t = align_up(t + 4 * (size_t)nb1);
   p->t_scan = t;
   t = align_up(t + 4 * scan_tmp_words(nk1));
+  p->t_fscale = t;
+  t = align_up(t + 8 * (size_t)g.C);
   const size_t bind_temp = t;
   // call temporaries
   size_t c = 0;
@@ -911,15 +922,18 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   const int64_t nk = nb * g.S;  // sort keys
   GB_CUDA(cudaMemsetAsync(counts, 0, 4 * (size_t)(nk + 1), s));
   GB_CUDA(cudaMemsetAsync(p->status_word(), 0, 4, s));
+  double *fscale = reinterpret_cast<double *>(tmp + p->t_fscale);
+  k_freq_scale<<<(g.C + kThreads - 1) / kThreads, kThreads, 0, s>>>(p->freq, g.C, fscale);
+  GB_LAUNCH_CHECK("k_freq_scale");
   if (g.shifted) {
     GB_CUDA(cudaMemcpyAsync(p->at<double>(p->off_coords), p->uvw, 24 * (size_t)g.R,
                             cudaMemcpyDeviceToDevice, s));
-    GB_CUDA(cudaMemcpyAsync(p->at<double>(p->off_coords) + 3 * (size_t)g.R, p->freq,
+    GB_CUDA(cudaMemcpyAsync(p->at<double>(p->off_coords) + 3 * (size_t)g.R, fscale,
                             8 * (size_t)g.C, cudaMemcpyDeviceToDevice, s));
   }
   {
     ProfScope ps(kProfCountKernel, s, rows + 8.0 * ni);
-    k_count<<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, counts, keys, ranks);
+    k_count<<<item_blocks, kThreads, 0, s>>>(g, p->uvw, fscale, counts, keys, ranks);
     GB_LAUNCH_CHECK("k_count");
   }
   int rc;
@@ -930,7 +944,7 @@ static int run_bind(gb_plan *p, cudaStream_t s) {
   if (rc) return rc;
   {
     ProfScope ps(kProfScatter, s, rows + ni * (12.0 + sizeof(Item)));
-    k_scatter<R><<<item_blocks, kThreads, 0, s>>>(g, p->uvw, p->freq, keys, ranks, offsets,
+    k_scatter<R><<<item_blocks, kThreads, 0, s>>>(g, p->uvw, fscale, keys, ranks, offsets,
                                                    items);
     GB_LAUNCH_CHECK("k_scatter");
   }

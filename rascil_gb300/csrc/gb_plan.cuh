@@ -26,7 +26,7 @@ struct gb_plan {
          off_tables = 0, off_counters = 0, off_fftwork = 0, off_temp = 0;
   // bind-time temporaries (inside the temp region)
   size_t t_keys = 0, t_ranks = 0, t_counts = 0, t_offsets = 0, t_ccounts = 0,
-         t_scan = 0;
+         t_scan = 0, t_fscale = 0;
   // call-time temporaries (inside the temp region)
   size_t c_grid = 0, c_img = 0, c_cvis = 0;
   size_t max_chunks = 0;
@@ -45,7 +45,7 @@ struct gb_plan {
   size_t off_rowmask = 0, off_twx = 0;
   int row_blocks = 0;
   size_t off_tprime = 0;  // [ny][nx] float64: n - 1 - tc per pixel (w-stacking)
-  size_t off_coords = 0;  // shifted plans: [R][3] uvw then [C] freq, float64
+  size_t off_coords = 0;  // shifted plans: [R][3] uvw then [C] f/c, float64
   // column mode: [ny][nx] w-screen phases as 64-bit fixed-point turns
   // (A, D), plane k's phase = A + k D mod 1; [ngy] exp(+2 pi i m / ngy)
   size_t off_screen = 0, off_twn = 0;

@@ -354,13 +354,29 @@ def _invert(bvis, model, dopsf, normalise, residual_of, kwargs):
         zeros = numpy.zeros(model["pixels"].data.shape, dtype=model["pixels"].data.dtype)
         return model.copy(deep=True, pixels=zeros), numpy.zeros([nchan, npol])
     uvw = _device_uvw(bvis.uvw.data, device)
-    vis = None
-    if not dopsf:
-        vis = _to_device(bvis["vis"].data.reshape(R, vnchan, vnpol), cdt, device)
-    flags = _to_device(bvis["flags"].data.reshape(R, vnchan, vnpol), None, device)
-    if flags.dtype != torch.int64:
-        flags = (flags != 0).to(torch.uint8)
-    wgt = _to_device(bvis["imaging_weight"].data.reshape(R, vnchan, vnpol), rdt, device)
+    # the visibilities, flags and weights (several times the uvw bytes) are
+    # uploaded on a side stream while this stream builds the plan (bucket
+    # sort); the gridding waits for them
+    main = torch.cuda.current_stream(device)
+    side = torch.cuda.Stream(device)
+    side.wait_stream(main)
+    with torch.cuda.stream(side):
+        vis = None
+        if not dopsf:
+            vis = _to_device(bvis["vis"].data.reshape(R, vnchan, vnpol), cdt, device)
+        flags = _to_device(bvis["flags"].data.reshape(R, vnchan, vnpol), None, device)
+        if flags.dtype != torch.int64:
+            flags = (flags != 0).to(torch.uint8)
+        wgt = _to_device(bvis["imaging_weight"].data.reshape(R, vnchan, vnpol), rdt, device)
+    uploaded = [t for t in (vis, flags, wgt) if t is not None]
+    for t in uploaded:  # allocated on the side stream, used on this one
+        t.record_stream(main)
+    joined = [False]
+
+    def join_uploads():
+        if not joined[0]:
+            main.wait_stream(side)
+            joined[0] = True
 
     pdt = model["pixels"].data.dtype
     acc = torch.zeros((nchan, npol, ny, nx), dtype=torch.float64, device=device)
@@ -381,6 +397,7 @@ def _invert(bvis, model, dopsf, normalise, residual_of, kwargs):
         key, entry = _checkout_plan(uvw, f, nx, ny, pixsize, epsilon, do_wstacking, npol,
                                     precision, shift, _budget(kwargs))
         try:
+            join_uploads()
             gvis = pick(vis)
             if residual_of is not None:
                 img = _to_device(residual_of["pixels"].data[ichan], rdt, device)
