@@ -1,10 +1,11 @@
 """GPU parity of the FP32 column-transform path (fused, pruned four-step
 column FFTs with the w-screen folded in; predict grids in permuted row
 order).  Small images are checked against the FP64 direct sum (oracle) at
-the FP32 bar, 1e-5 relative RMS; tall, ragged and multi-pol images
-against the plain FP64 GPU form, which is itself held to 1e-10 against
-the direct sum, at the same bar; and the two FP32 modes against each
-other."""
+the FP32 bar, 1e-5 relative RMS; tall, ragged, wide-grid and multi-pol
+images against the plain FP64 GPU form, which is itself held to 1e-10
+against the direct sum, at the same bar, and the tall and wide-grid ones
+also against the CPU oracle's direct sums at sampled pixels and rows; and
+the two FP32 modes against each other."""
 import numpy
 import pytest
 
@@ -19,6 +20,22 @@ TOL = 1e-5
 
 def _dev(x, dtype):
     return torch.from_numpy(numpy.ascontiguousarray(x)).to("cuda", dtype)
+
+
+def _check_oracle_samples(c, nx, ny, dirty, img, vis, nsample=64, seed=99):
+    """An FP32 dirty image ([1][x][y]) and prediction ([nrow][nchan][1]) of
+    the Stokes-I problem `c` against the CPU oracle's exact direct sums at
+    `nsample` random pixels and rows, at the FP32 bar."""
+    rng = numpy.random.default_rng(seed)
+    ix = rng.integers(0, nx, nsample)
+    iy = rng.integers(0, ny, nsample)
+    ref = dft.ms2dirty_dft(c["uvw"], c["freq"], c["ms"][..., 0], None, nx, ny, c["pixsize"],
+                           c["pixsize"], True, pixel_subset=(ix, iy))
+    assert rel_rms(dirty[0, ix, iy], ref) < TOL
+    rows = numpy.sort(rng.choice(c["uvw"].shape[0], nsample, replace=False))
+    vref = dft.dirty2ms_dft(c["uvw"], c["freq"], img[0], None, c["pixsize"], c["pixsize"], True,
+                            row_subset=rows, chunk=16)
+    assert rel_rms(vis[rows, :, 0], vref) < TOL
 
 
 def _plan(c, nx, ny, do_w, precision, fft_mode, npol=1, eps=1e-5, **kw):
@@ -92,6 +109,7 @@ def test_tall_images_vs_fp64(nx, ny):
     v32 = pf.dirty2ms(_dev(img, torch.float32)).cpu().numpy()
     v64 = pd.dirty2ms(_dev(img, torch.float64)).cpu().numpy()
     assert rel_rms(v32, v64) < TOL
+    _check_oracle_samples(c, nx, ny, dirty32, img, v32)
     assert pf.device_status() == 0
     pf.close()
     pd.close()
@@ -158,6 +176,7 @@ def test_row_kernel_vs_fp64(nx, ny):
     v32 = pf.dirty2ms(_dev(img, torch.float32)).cpu().numpy()
     v64 = pd.dirty2ms(_dev(img, torch.float64)).cpu().numpy()
     assert rel_rms(v32, v64) < TOL
+    _check_oracle_samples(c, nx, ny, d32, img, v32)
     assert pf.device_status() == 0
     pf.close()
     pd.close()

@@ -123,6 +123,15 @@ def test_small_array_predict_matches_exact_dft(precision, eps, tol):
     got = predict_ng(bvis, model, epsilon=eps, precision=precision)["vis"].data
     truth = bvis["vis"].data.astype(numpy.complex128)  # exact DFT of the same sources
     assert rel_rms(got, truth) < tol
+    # and directly against the CPU oracle's component DFT at sampled rows
+    from rascil_gb300 import simulation as sim
+    nchan = len(freq)
+    rows = numpy.sort(numpy.random.default_rng(1).choice(uvw.shape[0] * uvw.shape[1], 48,
+                                                         replace=False))
+    uvw_l = (uvw.reshape(-1, 3)[rows][None, :, None, :]
+             * (freq / odft.SPEED_OF_LIGHT)[None, None, :, None])
+    ref = odft.dft_cpu_looped(sim.lmn_rows(src), uvw_l, sim.component_fluxes(cfg, src, nchan))
+    assert rel_rms(got.reshape(-1, nchan, got.shape[-1])[rows], ref[0]) < tol
 
 
 def test_per_channel_path_and_flags():
