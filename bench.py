@@ -74,6 +74,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-planes", type=int, default=4,
                     help="w-planes in the CPU baseline sample")
+    ap.add_argument("--ref-planes", type=int, default=2,
+                    help="w-planes in each step's sample of --impl reference (the driver runs "
+                         "25 such steps, so a step is kept near 8 s on 16 cores)")
     ap.add_argument("--grid-budget-gb", type=float, default=0.0,
                     help="memory for one batch of w-planes (0 = planner default)")
     ap.add_argument("--fp64-warmup", type=int, default=0,
@@ -1493,7 +1496,7 @@ def run_reference(args):
     cw = CpuWorkload(args.config, args.scale)
     samples = []
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(cw, args.cpu_planes)
+        r = cpu_sample(cw, args.ref_planes)
         if i >= args.warmup:
             samples.append(r)
     t_sample = float(numpy.mean([r["sample_s"] for r in samples]))
