@@ -506,7 +506,7 @@ def cpu_choose_sigma(u, v, w, npix, cell, eps, cores, nplanes_probe=2, sigmas=CP
     return min(est, key=est.get), est
 
 
-def cpu_sample(cw, nplanes_sample):
+def cpu_sample(cw, nplanes_sample, nplanes_probe=2):
     """Invert + predict of the full workload restricted to an evenly spread
     subset of w-planes, one polarisation, FP64 on all host cores, at the
     oversampling fastest on the CPU.  Host only (``cw`` is a CpuWorkload):
@@ -524,7 +524,8 @@ def cpu_sample(cw, nplanes_sample):
     key = (cw.name, cw.scale)
     if key not in _CPU_SIGMA:
         try:
-            _CPU_SIGMA[key] = cpu_choose_sigma(u, v, w, cw.npixel, cw.cell, cw.epsilon, cores)
+            _CPU_SIGMA[key] = cpu_choose_sigma(u, v, w, cw.npixel, cw.cell, cw.epsilon, cores,
+                                               nplanes_probe)
         except (ValueError, IndexError, OSError) as e:  # an optimisation: keep the default
             print("cpu_choose_sigma failed (%s); the CPU baseline uses sigma 2" % e,
                   file=sys.stderr)
@@ -1496,7 +1497,7 @@ def run_reference(args):
     cw = CpuWorkload(args.config, args.scale)
     samples = []
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(cw, args.ref_planes)
+        r = cpu_sample(cw, args.ref_planes, nplanes_probe=1)
         if i >= args.warmup:
             samples.append(r)
     t_sample = float(numpy.mean([r["sample_s"] for r in samples]))

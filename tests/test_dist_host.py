@@ -46,7 +46,7 @@ def _reference_worker(rank, world, port, q):
 
     import bench
     args = argparse.Namespace(gpus=world, config="small-array", scale="tiny", warmup=3, steps=1,
-                              cpu_planes=1)
+                              cpu_planes=1, ref_planes=1)
     out = io.StringIO()
     with contextlib.redirect_stdout(out):
         bench.run_reference(args)
