@@ -75,8 +75,8 @@ def parse():
     ap.add_argument("--cpu-planes", type=int, default=4,
                     help="w-planes in the CPU baseline sample")
     ap.add_argument("--ref-planes", type=int, default=2,
-                    help="w-planes in each step's sample of --impl reference (the driver runs "
-                         "25 such steps, so a step is kept near 8 s on 16 cores)")
+                    help="w-planes in each step's sample of --impl reference (about 4-8 s a "
+                         "step on 16 cores, so 25 steps end within a few minutes)")
     ap.add_argument("--grid-budget-gb", type=float, default=0.0,
                     help="memory for one batch of w-planes (0 = planner default)")
     ap.add_argument("--fp64-warmup", type=int, default=0,
