@@ -1670,7 +1670,7 @@ def main():
         # host only: a failure of the CPU gridder is reported in the line and
         # does not abort the GPU measurement (no device work in this block)
         try:
-            r = cpu_sample(cw, args.cpu_planes)
+            r = cpu_sample(cw, args.cpu_planes, nplanes_probe=1)
             line["cpu_baseline"] = {"value": round(r["mvis"], 4), "unit": "Mvis/s",
                                     "cores": r["cores"], "kind": "port", "sample": r["desc"]}
             cpu_sigma = r["sigma"]
